@@ -1,0 +1,99 @@
+"""Build and load libkmc_gb300.so (the C ABI declared in include/kmc_gb300.h).
+
+The library is compiled in-tree for sm_103a with nvcc.  There is no CPU
+fallback: if the library cannot be built or loaded, every entry point raises.
+"""
+import ctypes
+import os
+import shutil
+import subprocess
+from ctypes import POINTER, c_char_p, c_double, c_int, c_int32, c_int64, c_void_p
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+_ROOT = os.path.dirname(_PKG)
+BUILD_DIR = os.path.join(_PKG, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "libkmc_gb300.so")
+SOURCES = [os.path.join(_PKG, "csrc", "kmc_gb300.cu")]
+DEPS = SOURCES + [os.path.join(_PKG, "csrc", "kmc_sph.cuh"), os.path.join(_ROOT, "include", "kmc_gb300.h")]
+ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+KMC_BC = {"free_space": 0, "27": 1, "pbc": 2}
+KMC_PREC = {"fp64": 0, "mixed": 1}
+KMC_ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "not initialised", -4: "bad proposed move",
+              -5: "cell store overflow", -6: "out of memory"}
+
+
+class KmcParams(ctypes.Structure):
+    _fields_ = [
+        ("boundary", c_int32), ("r", c_int32), ("l", c_int32), ("precision", c_int32),
+        ("extent", c_double), ("max_move", c_double), ("energy_unit", c_double),
+        ("lr_nnz", c_int64), ("lr_data", POINTER(c_double)), ("lr_indptr", POINTER(c_int64)),
+        ("lr_indices", POINTER(c_int64)), ("lr_dipole", c_double * 3),
+    ]
+
+
+def _nvcc():
+    nv = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nv):
+        raise RuntimeError("nvcc not found: the CUDA library cannot be built")
+    return nv
+
+
+def build(force=False, verbose=False):
+    """Compile libkmc_gb300.so for sm_103a (no GPU needed)."""
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if not force and os.path.exists(LIB_PATH):
+        lib_m = os.path.getmtime(LIB_PATH)
+        if all(os.path.getmtime(d) <= lib_m for d in DEPS):
+            return LIB_PATH
+    tmp = LIB_PATH + ".tmp"
+    cmd = [_nvcc(), *ARCH_FLAGS, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
+           "-I" + os.path.join(_ROOT, "include"), "-o", tmp, *SOURCES]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed:\n" + r.stdout + r.stderr)
+    if verbose:
+        print(r.stdout + r.stderr)
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+_lib = None
+
+# every exported symbol with its ctypes signature (argtypes, restype)
+SIGNATURES = {
+    "kmc_create": ([POINTER(KmcParams), POINTER(c_void_p)], c_int),
+    "kmc_set_stream": ([c_void_p, c_void_p], c_int),
+    "kmc_initialise": ([c_void_p, c_int64, c_void_p, c_void_p, POINTER(c_double)], c_int),
+    "kmc_propose_with_dats": ([c_void_p, c_int64, c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
+                               c_void_p, c_void_p], c_int),
+    "kmc_propose_moves": ([c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p], c_int),
+    "kmc_accept": ([c_void_p, c_int64, POINTER(c_double)], c_int),
+    "kmc_accept_device": ([c_void_p, c_void_p, c_void_p, c_void_p], c_int),
+    "kmc_get_energy": ([c_void_p, POINTER(c_double)], c_int),
+    "kmc_get_error": ([c_void_p, POINTER(c_int64), POINTER(c_int64)], c_int),
+    "kmc_read_state": ([c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p], c_int),
+    "kmc_info": ([c_void_p, POINTER(c_int64), POINTER(c_int64), POINTER(c_int64)], c_int),
+    "kmc_free": ([c_void_p], c_int),
+    "kmc_last_error": ([], c_char_p),
+}
+
+
+def lib():
+    """Load the library (building it first if needed); raises if unavailable."""
+    global _lib
+    if _lib is None:
+        path = build()
+        L = ctypes.CDLL(path)
+        for name, (argt, rest) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.argtypes = argt
+            f.restype = rest
+        _lib = L
+    return _lib
+
+
+def check(rc, what):
+    if rc != 0:
+        msg = lib().kmc_last_error().decode(errors="replace")
+        raise RuntimeError(f"{what} failed: {KMC_ERRORS.get(rc, rc)} ({msg})")

@@ -1,0 +1,351 @@
+"""KMCFMM: the user-facing FMM-KMC interface, GB300 implementation.
+
+Same constructor and methods as coulomb_kmc.KMCFMM (coulomb_kmc/kmc_fmm.py:436-1105):
+``initialise``, ``propose``, ``propose_with_dats``, ``accept``, ``free`` and the
+``energy`` attribute.  All arithmetic runs in libkmc_gb300.so on the current
+CUDA device; PyTorch only provides device buffers and the stream.  There is no
+CPU fallback.
+
+Inputs may be ppmd-style dats (anything with ``.data``), numpy arrays, or, for
+``propose_with_dats``, torch CUDA tensors (then nothing is copied between host
+and device).
+"""
+import ctypes
+from ctypes import byref, c_double, c_int64, c_void_p, POINTER
+from math import ceil, log
+
+import numpy as np
+
+from . import _native
+from .common import BCType
+from .dats import array_of, _is_torch
+from .lattice import lattice_operator
+
+REAL = ctypes.c_double
+INT64 = ctypes.c_int64
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _host(a, dtype):
+    if _is_torch(a):
+        a = a.detach().cpu().numpy()
+    return np.ascontiguousarray(np.asarray(a), dtype=dtype)
+
+
+class KMCFMM:
+    """Electrostatic energy differences for kinetic Monte Carlo (see coulomb_kmc.KMCFMM).
+
+    :arg positions: PositionDat (n,3) float64, numpy array or tensor of charge positions.
+    :arg charges: ParticleDat (n,1) float64 (or array) of charge values.
+    :arg domain: object with ``extent`` (cubic box [-E/2, E/2]^3), or the edge length.
+    :arg N: number of charges (optional; taken from ``positions``).
+    :arg boundary_condition: 'pbc', 'free_space' or '27'.
+    :arg r: number of FMM levels (finest level has 2^(r-1) cells per side).  Default
+        max(2, ceil(log8(N/8))).
+    :arg l: number of expansion terms (default 12).
+    :arg max_move: maximum per-axis displacement of a proposed move (default: box edge).
+    :arg energy_unit: multiplies all energies.
+    :arg precision: 'fp64' (default, the drop-in).
+    ``shell_width``, ``_debug`` and ``cuda_direct`` are accepted for signature
+    compatibility and have no effect (the whole path always runs on the GPU).
+    """
+
+    def __init__(self, positions, charges, domain, N=None, boundary_condition="pbc", r=None, shell_width=0.0,
+                 energy_unit=1.0, _debug=False, l=None, max_move=None, cuda_direct=False, mirror_direction=None,
+                 precision="fp64"):
+        self._bc = BCType(boundary_condition)
+        self.boundary_condition = self._bc
+        if self._bc == BCType.FF_ONLY:
+            raise NotImplementedError("boundary_condition='ff-only' is not part of this implementation")
+        if mirror_direction is not None:
+            raise NotImplementedError("mirror charges (Dirichlet boundaries) are not part of this implementation")
+        self.positions = positions
+        self.charges = charges
+        self.domain = domain
+        self.group = getattr(positions, "group", None)
+        ext = np.atleast_1d(np.asarray(getattr(domain, "extent", domain), dtype=np.float64))
+        if ext.size == 1:
+            ext = np.repeat(ext, 3)
+        if not (abs(ext[0] - ext[1]) < 1e-14 and abs(ext[0] - ext[2]) < 1e-14):
+            raise ValueError("only cubic domains are supported")
+        self.extent = float(ext[0])
+        pos = array_of(positions)
+        n = int(pos.shape[0]) if N is None else int(N)
+        self.N = n
+        if r is None:
+            r = max(2, int(ceil(log(max(n / 8.0, 1.0), 8)))) if n > 8 else 2
+        self.R = int(r)
+        self.L = int(l) if l is not None else 12
+        self.energy_unit = float(energy_unit)
+        self.max_move = float(max_move) if max_move is not None else float(np.max(ext))
+        self.cuda_direct = cuda_direct
+        self.precision = precision
+        self._energy = None
+        self._energy_valid = False
+        self._handle = None
+        self._staging = {}
+        L = _native.lib()
+        prm = _native.KmcParams()
+        prm.boundary = _native.KMC_BC[self._bc.value]
+        prm.r = self.R
+        prm.l = self.L
+        prm.precision = _native.KMC_PREC[precision]
+        prm.extent = self.extent
+        prm.max_move = self.max_move
+        prm.energy_unit = self.energy_unit
+        if self._bc == BCType.PBC:
+            data, indptr, indices, dip = lattice_operator(self.L, self.extent)
+            self._lr = (data, indptr, indices, dip)
+            prm.lr_nnz = len(data)
+            prm.lr_data = data.ctypes.data_as(POINTER(c_double))
+            prm.lr_indptr = indptr.ctypes.data_as(POINTER(c_int64))
+            prm.lr_indices = indices.ctypes.data_as(POINTER(c_int64))
+            for i in range(3):
+                prm.lr_dipole[i] = dip[i]
+        h = c_void_p()
+        _native.check(L.kmc_create(byref(prm), byref(h)), "kmc_create")
+        self._handle = h
+
+    # ------------------------------------------------------------------
+    @property
+    def energy(self):
+        """Total system energy (valid after initialise)."""
+        if self._handle is None or self._energy is None:
+            return self._energy
+        if not self._energy_valid:
+            e = c_double()
+            _native.check(_native.lib().kmc_get_energy(self._handle, byref(e)), "kmc_get_energy")
+            self._energy = e.value
+            self._energy_valid = True
+        return self._energy
+
+    def _assert_init(self):
+        if self._energy is None:
+            raise RuntimeError("Run initialise before this call")
+
+    def _set_stream(self):
+        torch = _torch()
+        if torch.cuda.is_available():
+            _native.lib().kmc_set_stream(self._handle, c_void_p(torch.cuda.current_stream().cuda_stream))
+
+    def initialise(self):
+        """Initial solve: cell store, finest-level local expansions, energy (kmc_fmm.py:947-993)."""
+        pos = _host(array_of(self.positions), np.float64).reshape(-1, 3)
+        q = _host(array_of(self.charges), np.float64).reshape(-1)
+        if pos.shape[0] != self.N or q.shape[0] != self.N:
+            raise ValueError("positions and charges must have N entries")
+        self._check_in_box(pos)
+        self._set_stream()
+        e = c_double()
+        _native.check(_native.lib().kmc_initialise(self._handle, self.N, pos.ctypes.data, q.ctypes.data, byref(e)),
+                      "kmc_initialise")
+        self._energy = e.value
+        self._energy_valid = True
+        self._charges_host = q
+
+    def _check_in_box(self, pos):
+        h = 0.5 * self.extent
+        if np.any(pos < -h) or np.any(pos > h):
+            raise RuntimeError("Charge position is outside simulation domain.")
+
+    def _positions_host(self):
+        return array_of(self.positions)
+
+    def _check_move_valid(self, old_pos, new_pos):
+        """kmc_mpi_decomp.py:312-345"""
+        e = self.extent
+        for d in range(3):
+            if np.any(new_pos[:, d] < -0.5 * e) or np.any(new_pos[:, d] > 0.5 * e):
+                raise RuntimeError("Proposed position is outside simulation domain. Extent {}, dimension {}, "
+                                   "value {}.".format(e, d, new_pos[:, d]))
+        periodic = self._bc != BCType.FREE_SPACE
+        for mx in new_pos:
+            rvec = mx - old_pos
+            if periodic:
+                for d in range(3):
+                    if rvec[d] < -0.5 * e:
+                        rvec[d] += e
+                    if rvec[d] > 0.5 * e:
+                        rvec[d] -= e
+            if np.any(np.abs(rvec) > self.max_move):
+                raise RuntimeError("Proposed move violates max_move. Old position {}, new position {}.".format(
+                    old_pos, mx))
+
+    # ------------------------------------------------------------------
+    def propose(self, moves):
+        """Total energies of proposed moves: moves = ((id, (k,3) array), ...) (kmc_fmm.py:774-787)."""
+        self._assert_init()
+        nump = len(moves)
+        movs = [np.atleast_2d(np.asarray(m[1], dtype=np.float64)) for m in moves]
+        pids = np.array([int(m[0]) for m in moves], dtype=np.int64)
+        counts = np.array([m.shape[0] for m in movs], dtype=np.int64)
+        es = np.zeros(nump + 1, dtype=np.int64)
+        es[1:] = np.cumsum(counts)
+        pos = self._positions_host()
+        pos_h = _host(pos, np.float64).reshape(-1, 3)
+        for pid, mv in zip(pids, movs):
+            self._check_move_valid(pos_h[pid], mv)
+        newp = np.ascontiguousarray(np.concatenate(movs, axis=0), dtype=np.float64)
+        diffs = np.zeros(int(es[-1]), dtype=np.float64)
+        self._set_stream()
+        _native.check(_native.lib().kmc_propose_moves(self._handle, nump, pids.ctypes.data, es.ctypes.data,
+                                                      newp.ctypes.data, diffs.ctypes.data), "kmc_propose_moves")
+        energy = self.energy
+        out = []
+        for i, (pid, mv) in enumerate(zip(pids, movs)):
+            e = np.zeros(mv.shape[0])
+            for j, mx in enumerate(mv):
+                if np.linalg.norm(pos_h[pid, :] - mx) < 10.0 ** -14:
+                    e[j] = energy
+                else:
+                    e[j] = energy + diffs[es[i] + j]
+            out.append(e)
+        return tuple(out)
+
+    # ------------------------------------------------------------------
+    def _stage(self, name, arr_np, torch_dtype):
+        """Copy a host array into a persistent pinned -> device staging pair."""
+        torch = _torch()
+        n = arr_np.size
+        buf = self._staging.get(name)
+        if buf is None or buf[0].numel() < n:
+            h = torch.empty(max(n, 1), dtype=torch_dtype, pin_memory=True)
+            d = torch.empty(max(n, 1), dtype=torch_dtype, device="cuda")
+            buf = (h, d)
+            self._staging[name] = buf
+        h, d = buf
+        h[:n].numpy()[:] = arr_np.reshape(-1)
+        d[:n].copy_(h[:n], non_blocking=True)
+        return d
+
+    def propose_with_dats(self, site_max_counts, current_sites, prop_positions, prop_masks, prop_energy_diffs,
+                          diff=True, prop_charges=None, sync=True):
+        """Energy differences of masked proposals written into prop_energy_diffs (kmc_fmm.py:665-762).
+
+        With torch CUDA tensors for all arrays the call is device resident; ``sync=False`` then skips
+        the host read of the move-validation counter (call ``check_errors()`` later).
+        """
+        self._assert_init()
+        if not diff:
+            raise NotImplementedError()
+        smc, sites = array_of(site_max_counts), array_of(current_sites)
+        ppos, pmask, pde = array_of(prop_positions), array_of(prop_masks), array_of(prop_energy_diffs)
+        pq = array_of(prop_charges) if prop_charges is not None else None
+        M = int(pmask.shape[1])
+        if int(pde.shape[1]) != M or int(ppos.shape[1]) != 3 * M:
+            raise AssertionError("prop_energy_diffs/prop_positions strides must match prop_masks")
+        nsite = int(np.prod(smc.shape))
+        L = _native.lib()
+        self._set_stream()
+        if all(_is_torch(a) and a.is_cuda for a in (smc, sites, ppos, pmask, pde)) and \
+                (pq is None or (_is_torch(pq) and pq.is_cuda)):
+            torch = _torch()
+            for a, dt in ((smc, torch.int64), (sites, torch.int64), (pmask, torch.int64), (ppos, torch.float64),
+                          (pde, torch.float64)):
+                if a.dtype != dt or not a.is_contiguous():
+                    raise TypeError("device dats must be contiguous int64/float64 tensors")
+            _native.check(L.kmc_propose_with_dats(self._handle, self.N, M, nsite, smc.data_ptr(), sites.data_ptr(),
+                                                  ppos.data_ptr(), pmask.data_ptr(),
+                                                  pq.data_ptr() if pq is not None else None, pde.data_ptr()),
+                          "kmc_propose_with_dats")
+            if sync:
+                self.check_errors()
+            return
+        torch = _torch()
+        d_smc = self._stage("smc", _host(smc, np.int64), torch.int64)
+        d_sites = self._stage("sites", _host(sites, np.int64), torch.int64)
+        d_ppos = self._stage("ppos", _host(ppos, np.float64), torch.float64)
+        d_mask = self._stage("mask", _host(pmask, np.int64), torch.int64)
+        d_pde = self._stage("pde", _host(pde, np.float64), torch.float64)
+        d_pq = self._stage("pq", _host(pq, np.float64), torch.float64) if pq is not None else None
+        _native.check(L.kmc_propose_with_dats(self._handle, self.N, M, nsite, d_smc.data_ptr(), d_sites.data_ptr(),
+                                              d_ppos.data_ptr(), d_mask.data_ptr(),
+                                              d_pq.data_ptr() if d_pq is not None else None, d_pde.data_ptr()),
+                      "kmc_propose_with_dats")
+        h_pde = self._staging["pde"][0]
+        n = self.N * M
+        h_pde[:n].copy_(d_pde[:n], non_blocking=True)
+        self.check_errors()  # synchronises the stream
+        out = h_pde[:n].numpy().reshape(pde.shape)
+        if _is_torch(pde):
+            pde.copy_(torch.from_numpy(out))
+        else:
+            pde[...] = out
+
+    def check_errors(self):
+        """Raise RuntimeError if any proposed move since the last check was invalid."""
+        bad, ovf = c_int64(), c_int64()
+        _native.check(_native.lib().kmc_get_error(self._handle, byref(bad), byref(ovf)), "kmc_get_error")
+        if ovf.value > 0:
+            raise RuntimeError("A cell store overflowed during a device-selected accept.")
+        if bad.value > 0:
+            raise RuntimeError("Bad proposed move was detected.")
+
+    # ------------------------------------------------------------------
+    def accept(self, move=None):
+        """Accept move = (id, new_position): updates the energy, the GPU state and the positions dat
+        (kmc_fmm.py:789-912)."""
+        self._assert_init()
+        if move is None:
+            raise RuntimeError("No moves to accept were passed.")
+        pid = int(move[0])
+        newp = np.ascontiguousarray(np.asarray(move[1], dtype=np.float64).reshape(3))
+        pos = self._positions_host()
+        old = _host(pos[pid], np.float64).reshape(3)
+        self._check_move_valid(old, newp.reshape(1, 3))
+        self._set_stream()
+        _native.check(_native.lib().kmc_accept(self._handle, pid, newp.ctypes.data_as(POINTER(c_double))),
+                      "kmc_accept")
+        self._energy_valid = False
+        if _is_torch(pos):
+            pos[pid, :] = _torch().from_numpy(newp).to(pos.device)
+        else:
+            pos[pid, :] = newp
+
+    def accept_device(self, d_pid, d_new_position, d_energy_diff):
+        """Accept a move selected on the device (int64[1], float64[3], float64[1] CUDA tensors).
+
+        Does not synchronise and does not update a host positions dat; read the
+        positions back with ``state()`` when needed."""
+        self._assert_init()
+        self._set_stream()
+        _native.check(_native.lib().kmc_accept_device(self._handle, d_pid.data_ptr(), d_new_position.data_ptr(),
+                                                      d_energy_diff.data_ptr()), "kmc_accept_device")
+        self._energy_valid = False
+
+    # ------------------------------------------------------------------
+    def state(self):
+        """Device state copied to host: positions, cells, occupancy, reference-layout local
+        expansions [ncell, 2L^2] and (pbc) the level-0 multipole."""
+        ncell, cap, n = c_int64(), c_int64(), c_int64()
+        L = _native.lib()
+        L.kmc_info(self._handle, byref(ncell), byref(cap), byref(n))
+        pos = np.zeros((n.value, 3))
+        cells = np.zeros(n.value, np.int64)
+        occ = np.zeros(ncell.value, np.int64)
+        lexp = np.zeros((ncell.value, 2 * self.L * self.L))
+        mp = np.zeros(2 * self.L * self.L)
+        _native.check(L.kmc_read_state(self._handle, pos.ctypes.data, cells.ctypes.data, occ.ctypes.data,
+                                       lexp.ctypes.data, mp.ctypes.data), "kmc_read_state")
+        return {"positions": pos, "cells": cells, "occupancy": occ, "local_expansions": lexp, "multipole": mp,
+                "capacity": cap.value}
+
+    def free(self):
+        """Release the GPU state (kmc_fmm.py:569-577)."""
+        if self._handle is not None:
+            _native.lib().kmc_free(self._handle)
+            self._handle = None
+        self._staging = {}
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def eval_field(self, points):
+        raise NotImplementedError("eval_field is not part of this implementation yet")

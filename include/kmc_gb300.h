@@ -1,0 +1,139 @@
+/*
+ * kmc_gb300.h -- C ABI of the GB300 FMM-KMC energy-difference library
+ * (libkmc_gb300.so).
+ *
+ * One handle = one KMC system (one cubic box of point charges) resident on
+ * the current CUDA device.  All entry points return KMC_OK (0) or a negative
+ * KMC_E* code; no C++ exception crosses this boundary.  A handle is bound to
+ * one CUDA stream (kmc_set_stream) and is not thread safe.
+ *
+ * Each entry point names the reference (ppmd/coulomb_kmc) interface it
+ * replaces; paths are relative to the coulomb_kmc project root.
+ */
+#ifndef KMC_GB300_H
+#define KMC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* boundary conditions: coulomb_kmc/common.py:37-50 (BCType) */
+#define KMC_BC_FREE_SPACE 0
+#define KMC_BC_NEAREST27 1 /* '27': primary box plus its 26 nearest images */
+#define KMC_BC_PBC 2
+
+/* arithmetic of the propose path */
+#define KMC_PREC_FP64 0  /* plain FP64 drop-in */
+#define KMC_PREC_MIXED 1 /* FP32 near field / expansion evaluation over FP32 copies */
+
+#define KMC_OK 0
+#define KMC_EINVAL -1     /* bad argument */
+#define KMC_ECUDA -2      /* CUDA runtime error */
+#define KMC_ESTATE -3     /* not initialised */
+#define KMC_EBADMOVE -4   /* proposed move outside the box or beyond max_move */
+#define KMC_EOVERFLOW -5  /* a cell store overflowed (device-selected accept) */
+#define KMC_ENOMEM -6
+
+typedef struct kmc_system kmc_system;
+
+typedef struct kmc_params {
+    int32_t boundary;     /* KMC_BC_* */
+    int32_t r;            /* FMM levels; the finest level has 2^(r-1) cells per side (r >= 2) */
+    int32_t l;            /* number of expansion terms, 2 <= l <= 32 */
+    int32_t precision;    /* KMC_PREC_* */
+    double extent;        /* cubic box edge; the box is [-extent/2, extent/2]^3 */
+    double max_move;      /* maximum per-axis displacement of a proposed move */
+    double energy_unit;   /* multiplies every energy */
+    /* KMC_BC_PBC only: far-field lattice operator (host memory, copied by kmc_create).
+       CSR over the l^2 x l^2 real operator acting on the real and imaginary blocks,
+       and the dipole correction -- the interface of ppmd's LongRangeMTL
+       (kmc_full_long_range.py:40, linop_data/linop_indptr/linop_indices, dipole_correction). */
+    int64_t lr_nnz;
+    const double *lr_data;
+    const int64_t *lr_indptr;
+    const int64_t *lr_indices;
+    double lr_dipole[3];
+} kmc_params;
+
+/* Create a system.  Replaces KMCFMM.__init__ (kmc_fmm.py:436-542) and the
+ * component constructors it wires (FMMMPIDecomp, LocalParticleData,
+ * LocalCellExpansions, FMMSelfInteraction, FullLongRangeEnergy). */
+int kmc_create(const kmc_params *params, kmc_system **out);
+
+/* Bind the handle to a CUDA stream (cudaStream_t passed as void*; NULL = legacy default). */
+int kmc_set_stream(kmc_system *s, void *stream);
+
+/* Initial solve: bins the charges, builds the cell store, the finest-level
+ * local expansions, the level-0 multipole (pbc) and the total energy.
+ * positions: host (n,3) f64, charges: host (n) f64.  energy_out: host, may be NULL.
+ * Replaces KMCFMM.initialise (kmc_fmm.py:947-993), including the PyFMM solve. */
+int kmc_initialise(kmc_system *s, int64_t n, const double *positions, const double *charges, double *energy_out);
+
+/* Energy differences of masked proposals, all pointers device memory.
+ * site_max_counts[n_site_types], current_sites[n], prop_positions[n][3*max_prop],
+ * prop_masks[n][max_prop], prop_charges[n][max_prop] or NULL,
+ * prop_energy_diffs[n][max_prop] (only active slots are written).
+ * Move validation errors are counted on the device; read them with
+ * kmc_get_error.  Replaces KMCFMM.propose_with_dats (kmc_fmm.py:665-762):
+ * setup_move (kmc_mpi_decomp.py:501-616), direct_new/direct_old
+ * (kmc_local.py:928-1031), indirect_interactions (kmc_octal.py:569-707),
+ * self_interaction (kmc_fmm_self_interaction.py:190-267), long_range_energy
+ * (kmc_full_long_range.py:710-858) and diff_lib (kmc_fmm.py:583-663). */
+int kmc_propose_with_dats(kmc_system *s, int64_t n, int64_t max_prop, int64_t n_site_types,
+                          const int64_t *site_max_counts, const int64_t *current_sites,
+                          const double *prop_positions, const int64_t *prop_masks, const double *prop_charges,
+                          double *prop_energy_diffs);
+
+/* Energy differences for explicit moves in CSR form (host memory):
+ * particle ids pids[nump], exclusive_sum[nump+1], new_positions[total][3];
+ * diffs_out[total] receives dE * energy_unit (host).  Synchronises.
+ * Replaces the component calls of KMCFMM._propose (kmc_fmm.py:1001-1105)
+ * after FMMMPIDecomp.setup_propose (kmc_mpi_decomp.py:238-310). */
+int kmc_propose_moves(kmc_system *s, int64_t nump, const int64_t *pids, const int64_t *exclusive_sum,
+                      const double *new_positions, double *diffs_out);
+
+/* Accept one move given on the host (pid, new position): the energy is
+ * advanced by that move's energy difference, the charge's position, cell and
+ * store slot are updated, every cell's local expansion and (pbc) the level-0
+ * multipole are updated.  Does not synchronise.
+ * Replaces KMCFMM.accept/_accept (kmc_fmm.py:789-912): LocalParticleData.accept
+ * (kmc_local.py:180-371), accept_local_exp (kmc_octal.py:961-1227),
+ * FullLongRangeEnergy.accept (kmc_full_long_range.py:270-316). */
+int kmc_accept(kmc_system *s, int64_t pid, const double new_position[3]);
+
+/* As kmc_accept, with the move read from device memory written by a device
+ * selection step: d_pid[1], d_new_position[3], d_energy_diff[1] (dE already
+ * multiplied by energy_unit, as written by kmc_propose_with_dats).  No host
+ * synchronisation; usable inside a captured CUDA graph. */
+int kmc_accept_device(kmc_system *s, const int64_t *d_pid, const double *d_new_position,
+                      const double *d_energy_diff);
+
+/* Current total energy (synchronises). */
+int kmc_get_energy(kmc_system *s, double *energy_out);
+
+/* Read and clear the device error counters (synchronises):
+ * bad_moves = invalid proposals since the last call, overflow = store overflows. */
+int kmc_get_error(kmc_system *s, int64_t *bad_moves, int64_t *overflow);
+
+/* Copy state to host for inspection (synchronises; any pointer may be NULL):
+ * positions[n][3], cells[n] (linear finest-level cell, x fastest),
+ * occupancy[ncell], local expansions in the reference layout [ncell][2 l^2],
+ * multipole[2 l^2] (pbc; reference layout). */
+int kmc_read_state(kmc_system *s, double *positions, int64_t *cells, int64_t *occupancy,
+                   double *local_expansions, double *multipole);
+
+/* Number of finest-level cells and the current store capacity per cell. */
+int kmc_info(kmc_system *s, int64_t *ncell, int64_t *capacity, int64_t *n);
+
+/* Release all device memory of the handle.  Replaces KMCFMM.free (kmc_fmm.py:569-577). */
+int kmc_free(kmc_system *s);
+
+/* Last CUDA error string of this thread's last failing call (static storage). */
+const char *kmc_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KMC_GB300_H */
