@@ -74,6 +74,10 @@ SIGNATURES = {
     "kmc_get_error": ([c_void_p, POINTER(c_int64), POINTER(c_int64)], c_int),
     "kmc_read_state": ([c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p], c_int),
     "kmc_info": ([c_void_p, POINTER(c_int64), POINTER(c_int64), POINTER(c_int64)], c_int),
+    "kmc_profile": ([c_void_p, c_int32], c_int),
+    "kmc_profile_read": ([c_void_p, c_int32, c_void_p, c_void_p, POINTER(c_int64)], c_int),
+    "kmc_kernel_name": ([c_int32], c_char_p),
+    "kmc_diag_fma_rate": ([c_int32, c_int32, POINTER(c_double)], c_int),
     "kmc_free": ([c_void_p], c_int),
     "kmc_last_error": ([], c_char_p),
 }
@@ -91,6 +95,9 @@ def lib():
             f.restype = rest
         _lib = L
     return _lib
+
+
+NKERNELS = 11
 
 
 def check(rc, what):

@@ -113,7 +113,9 @@ def make_state(positions, charges, extent):
 
 def array_of(obj):
     """The array behind a dat-like object (numpy array or torch tensor)."""
-    if hasattr(obj, "data") and not _is_torch(obj):
+    if isinstance(obj, np.ndarray) or _is_torch(obj):
+        return obj
+    if hasattr(obj, "data"):
         return obj.data
     return obj
 

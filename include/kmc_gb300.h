@@ -127,6 +127,22 @@ int kmc_read_state(kmc_system *s, double *positions, int64_t *cells, int64_t *oc
 /* Number of finest-level cells and the current store capacity per cell. */
 int kmc_info(kmc_system *s, int64_t *ncell, int64_t *capacity, int64_t *n);
 
+/* Per-kernel timing with CUDA events on the handle's stream (off by default).
+ * kmc_profile_read synchronises, and returns for every kernel id
+ * (0 <= id < KMC_NKERNELS, names from kmc_kernel_name) the accumulated
+ * milliseconds and launch counts since the last reset, and the number of kernel
+ * launches issued by this handle.  Counterpart of the reference's per-component
+ * timers in the PROFILE dictionary (common.py:136-160, kmc_fmm.py:894-912). */
+#define KMC_NKERNELS 11
+int kmc_profile(kmc_system *s, int32_t enable);
+int kmc_profile_read(kmc_system *s, int32_t reset, double *ms_out, int64_t *count_out, int64_t *launches_out);
+const char *kmc_kernel_name(int32_t id);
+
+/* Diagnostic (no reference counterpart): measured FMA throughput of the
+ * current device's FP64 (fp64 != 0) or FP32 pipe in TFLOP/s (FMA = 2 flops),
+ * the denominator of the roofline fraction of the FMA-bound kernels. */
+int kmc_diag_fma_rate(int32_t fp64, int32_t iters, double *tflops_out);
+
 /* Release all device memory of the handle.  Replaces KMCFMM.free (kmc_fmm.py:569-577). */
 int kmc_free(kmc_system *s);
 
