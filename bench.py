@@ -1,0 +1,432 @@
+"""Benchmark: proposal energy differences per second on the pbc lattice-hop workload.
+
+Workload (one system per GPU): simple-cubic lattice of 48^3 sites (spacing 1,
+box edge 48, periodic), 27,648 charges (25 % occupancy, +-1 balanced, seed 1),
+FMM depth R=5 (16^3 cells), L=12.  One step = one rejection-free KMC step:
+every charge proposes a hop to each vacant nearest-neighbour site (~124k
+proposals), all proposal energy differences are computed, one move is chosen
+with rate exp(-beta dE / 2), beta = 2, and accepted.
+
+Timed arms:
+  value : device resident -- proposals, masks, selection and bookkeeping on the
+          GPU (torch ops on device tensors) around the library's propose and
+          accept kernels; L2 flushed (256 MiB write) between timed steps.
+  e2e   : the reference-facing API with host (numpy) buffers, exactly as the
+          reference's driver uses it: host bookkeeping, propose_with_dats with
+          host<->device copies, host selection, accept.
+  --impl reference : the reference's CPU path as restated by the oracle
+          (ppmd/coulomb_kmc cannot be built here), all host threads.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Multi-GPU (torchrun): independent replicas, one system per rank, no collective
+on the data path; value = proposals over all ranks / max rank time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "proposal ΔE/sec, batched mixed-precision vs plain FP64 at ≤1e-6 rel err; p99"
+UNIT = "proposals/s"
+SIDE, OCC, R, L, BETA = 48, 0.25, 5, 12, 2.0
+
+
+def workload_config(side, precision):
+    n = int(round(OCC * side ** 3))
+    return {"workload": f"pbc lattice-hop {side}^3 sites, {n - n % 2} charges (25% occupied, +-1), "
+                        f"R={R}, L={L}, rejection-free KMC beta={BETA}, hops to vacant nearest neighbours",
+            "boundary_condition": "pbc", "R": R, "L": L, "sites_per_side": side, "precision": precision,
+            "l2": "state < L2; a 256 MiB buffer is written between timed steps (L2 flush)"}
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.strip().lower() in ("active", "1"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+class DeviceLattice:
+    """Lattice-hop bookkeeping on the device (torch), feeding the library's
+    device-resident propose_with_dats / accept_device."""
+
+    def __init__(self, host_sys, device):
+        import torch
+        self.t = torch
+        self.k = host_sys.side
+        self.E = host_sys.extent
+        self.n = host_sys.n
+        self.M = 6
+        self.site_of = torch.from_numpy(host_sys.site_of.copy()).to(device)
+        occ = np.full(self.k ** 3, -1, np.int64)
+        occ[host_sys.site_of] = np.arange(self.n)
+        self.occ = torch.from_numpy(occ).to(device)
+        self.hops = torch.tensor([(1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)],
+                                 dtype=torch.int64, device=device)
+        self.smc = torch.tensor([6], dtype=torch.int64, device=device)
+        self.sites = torch.zeros((self.n, 1), dtype=torch.int64, device=device)
+        self.diffs = torch.zeros((self.n, self.M), dtype=torch.float64, device=device)
+        self.ar = torch.arange(self.n, device=device)
+        self.gen = torch.Generator(device=device)
+        self.gen.manual_seed(1234)
+
+    def build(self):
+        t, k = self.t, self.k
+        s = self.site_of
+        xyz = torch_stack = t.stack((s % k, (s // k) % k, s // (k * k)), dim=1)
+        tgt = (torch_stack[:, None, :] + self.hops[None, :, :]) % k
+        self.tsite = tgt[..., 0] + k * (tgt[..., 1] + k * tgt[..., 2])
+        self.masks = (self.occ[self.tsite] < 0).to(t.int64)
+        self.ppos = (tgt.to(t.float64) - 0.5 * self.E + 0.5).reshape(self.n, 3 * self.M).contiguous()
+        del xyz
+
+    def select(self, beta):
+        t = self.t
+        rates = t.where(self.masks > 0, t.exp(-0.5 * beta * self.diffs), t.zeros_like(self.diffs)).reshape(-1)
+        c = t.cumsum(rates, 0)
+        u = t.rand(1, generator=self.gen, device=c.device, dtype=t.float64) * c[-1]
+        idx = t.searchsorted(c, u, right=True).clamp_(max=c.numel() - 1)
+        pid = idx // self.M
+        h = idx % self.M
+        self.d_pid = pid.contiguous()
+        self.d_new = self.ppos.view(self.n, self.M, 3)[pid, h].reshape(3).contiguous()
+        self.d_de = self.diffs.view(-1)[idx].contiguous()
+        self.new_site = self.tsite[pid, h]
+
+    def commit(self):
+        pid = self.d_pid
+        self.occ[self.site_of[pid]] = -1
+        self.occ[self.new_site] = pid
+        self.site_of[pid] = self.new_site
+
+    def step(self, kmc, beta):
+        self.build()
+        kmc.propose_with_dats(self.smc, self.sites, self.ppos, self.masks, self.diffs, sync=False)
+        self.select(beta)
+        kmc.accept_device(self.d_pid, self.d_new, self.d_de)
+        self.commit()
+        return self.n
+
+
+# ---------------------------------------------------------------------------
+def flop_model(kmc, host_sys, lr_nnz_folded):
+    """Algorithmic FP64 flops per launch for the step's kernels (add/mul = 1,
+    FMA = 2, rsqrt = 1), from this step's proposals and cell occupancy."""
+    st = kmc.state()
+    n = 2 ** (R - 1)
+    occ = st["occupancy"].reshape(n, n, n)
+    # sum over the 27 neighbour cells of each cell (periodic)
+    nb = np.zeros_like(occ)
+    for dz in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dx in (-1, 0, 1):
+                nb += np.roll(occ, shift=(dz, dy, dx), axis=(0, 1, 2))
+    nb = nb.reshape(-1)
+    ppos, masks, _ = host_sys.proposals()
+    act = masks.reshape(-1) > 0
+    pp = ppos.reshape(-1, 3)[act]
+    inv_w = n / host_sys.extent
+    c = np.minimum(((pp + 0.5 * host_sys.extent) * inv_w).astype(np.int64), n - 1)
+    pcell = c[:, 0] + n * (c[:, 1] + n * c[:, 2])
+    nh = L * (L + 1) // 2
+    far = 12 * nh + 6 * L                      # recurrence + coefficient dot products
+    nprop = int(act.sum())
+    movers = np.nonzero(masks.sum(axis=1) > 0)[0]
+    new_flops = float(np.sum(11 * nb[pcell])) + nprop * (far + 27 * 11 + 6)
+    old_flops = float(np.sum(11 * nb[st["cells"][movers]])) + len(movers) * (far + 2)
+    mpole = 12 * nh + 6 * L
+    lr_flops = nprop * (2 * mpole + 6 * nh + 2 * lr_nnz_folded + 2 * nh)
+    ncell = n ** 3
+    p2l = ncell * 54 * (L * 12 + 30)           # per (cell, source): l-chain per m + geometry
+    return {"new_side": new_flops, "old_side": old_flops, "far_lattice": lr_flops, "accept_p2l": p2l,
+            "proposals": nprop, "mean_neighbours": float(np.mean(nb[pcell]))}
+
+
+def kernel_times(kmc):
+    from ctypes import c_int64
+    from coulomb_kmc_gb300 import _native
+    lib = _native.lib()
+    ms = np.zeros(_native.NKERNELS)
+    cnt = np.zeros(_native.NKERNELS, np.int64)
+    launches = c_int64()
+    _native.check(lib.kmc_profile_read(kmc._handle, 1, ms.ctypes.data, cnt.ctypes.data, launches), "profile")
+    names = [lib.kmc_kernel_name(i).decode() for i in range(_native.NKERNELS)]
+    return {nm: (float(m), int(c)) for nm, m, c in zip(names, ms, cnt)}, launches.value
+
+
+def fma_peak(fp64=True):
+    from ctypes import c_double, byref
+    from coulomb_kmc_gb300 import _native
+    v = c_double()
+    _native.check(_native.lib().kmc_diag_fma_rate(1 if fp64 else 0, 20000 if fp64 else 200000, byref(v)), "diag")
+    return v.value
+
+
+def folded_nnz():
+    """Non-zeros of the folded lattice quadratic form (A_re + A_im), as the library builds it."""
+    from coulomb_kmc_gb300.lattice import dense_operator
+    Rm = dense_operator(L, float(SIDE))
+    nh = L * (L + 1) // 2
+    Ar = np.zeros((nh, nh))
+    Ai = np.zeros((nh, nh))
+    for j in range(L):
+        for k in range(-j, j + 1):
+            for nn in range(L):
+                for m in range(-nn, nn + 1):
+                    v = Rm[j * j + j + k, nn * nn + nn + m]
+                    if v == 0.0:
+                        continue
+                    hr, hc = j * (j + 1) // 2 + abs(k), nn * (nn + 1) // 2 + abs(m)
+                    Ar[hr, hc] += v
+                    Ai[hr, hc] += np.sign(k) * np.sign(m) * v
+    return int(np.count_nonzero(Ar) + np.count_nonzero(Ai) + 3)
+
+
+# ---------------------------------------------------------------------------
+def cpu_reference(steps, warmup, side, with_gpu_state=None):
+    """The reference's CPU path (oracle restatement, OpenMP on all host cores)."""
+    from oracle import kmc_oracle as ko
+    from coulomb_kmc_gb300.lattice import lattice_operator
+    from coulomb_kmc_gb300.workloads import LatticeHopSystem
+    hs = LatticeHopSystem(side, OCC, seed=1)
+    o = ko.OracleKMC(hs.positions(), hs.charges(), hs.extent, R, L, "pbc", max_move=1.0,
+                     lr_operator=lattice_operator(L, hs.extent))
+    ncell = (2 ** (R - 1)) ** 3
+    lexp = with_gpu_state if with_gpu_state is not None else np.zeros((ncell, 2 * L * L))
+    o.initialise(local_expansions=lexp)
+    rng = np.random.default_rng(3)
+    for _ in range(warmup):
+        hs.step(o, rng, BETA)
+    t0 = time.perf_counter()
+    nprop = 0
+    for _ in range(steps):
+        _, masks, _ = hs.proposals()
+        nprop += int(masks.sum())
+        hs.step(o, rng, BETA)
+    dt = time.perf_counter() - t0
+    return nprop / dt, dt, nprop
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = os.cpu_count()
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    steps = max(1, min(args.steps, args.ref_steps))
+    v, dt, nprop = cpu_reference(steps, min(args.warmup, 1), SIDE)
+    sample = (f"{steps} KMC steps of the {SIDE}^3 lattice-hop workload ({nprop} proposals), oracle restatement "
+              f"of the reference's generated C (ppmd is unavailable), OpenMP {cores} threads; "
+              f"initial expansions zero (the operation count does not depend on their values)")
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
+            "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(SIDE, "fp64"),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64"])
+    ap.add_argument("--side", type=int, default=SIDE)
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--cpu-steps", type=int, default=5)
+    ap.add_argument("--ref-steps", type=int, default=10)
+    ap.add_argument("--no-extras", action="store_true", help="timed loop only (for profiler runs)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 0)
+
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    import torch.distributed as dist
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from coulomb_kmc_gb300 import KMCFMM
+    from coulomb_kmc_gb300.dats import make_state
+    from coulomb_kmc_gb300.workloads import LatticeHopSystem
+
+    side = args.side
+    hs = LatticeHopSystem(side, OCC, seed=1 + rank)
+    st = make_state(hs.positions(), hs.charges(), hs.extent)
+    kmc = KMCFMM(st.P, st.Q, st.domain, r=R, l=L, boundary_condition="pbc", max_move=1.0)
+    t0 = time.perf_counter()
+    kmc.initialise()
+    init_s = time.perf_counter() - t0
+    dev = DeviceLattice(hs, torch.device("cuda", local))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    for _ in range(args.warmup):
+        dev.step(kmc, BETA)
+    torch.cuda.synchronize()
+    kmc.check_errors()
+    from coulomb_kmc_gb300 import _native
+    kernel_times(kmc)  # reset counters
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    nprop = 0
+    counts = []
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        ev[i][0].record()
+        dev.step(kmc, BETA)
+        ev[i][1].record()
+        counts.append(dev.masks.sum())
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    per_step = np.array([a.elapsed_time(b) for a, b in ev])
+    nprop = int(torch.stack(counts).sum().item())
+    _, launches = kernel_times(kmc)
+    kmc.check_errors()
+    t_ms = float(per_step.sum())
+    tot = torch.tensor([t_ms, float(nprop)], dtype=torch.float64, device="cuda")
+    if world > 1:
+        tmax = tot[0:1].clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        dist.all_reduce(tot[1:2], op=dist.ReduceOp.SUM)
+        tot[0] = tmax[0]
+    t_ms, nprop_all = float(tot[0]), float(tot[1])
+    value = nprop_all / (t_ms * 1e-3)
+
+    extras = {}
+    if not args.no_extras:
+        # per-kernel durations with CUDA events (separate pass so the timed loop is not perturbed)
+        _native.lib().kmc_profile(kmc._handle, 1)
+        kernel_times(kmc)
+        host_snapshot = LatticeHopSystem(side, OCC, seed=1 + rank)
+        host_snapshot.site_of = dev.site_of.cpu().numpy()
+        host_snapshot.occ[:] = -1
+        host_snapshot.occ[host_snapshot.site_of] = np.arange(host_snapshot.n)
+        fm = flop_model(kmc, host_snapshot, folded_nnz())
+        prof_steps = 5
+        for i in range(prof_steps):
+            flush.fill_(float(i))
+            dev.step(kmc, BETA)
+        kt, _ = kernel_times(kmc)
+        _native.lib().kmc_profile(kmc._handle, 0)
+        peak64 = fma_peak(True)
+        per_launch = {k: (v[0] / max(v[1], 1)) for k, v in kt.items() if v[1] > 0}
+        top = max(per_launch, key=lambda k: kt[k][0])
+        ach = {k: fm[k] / (per_launch[k] * 1e-3) / 1e12 for k in ("new_side", "old_side", "far_lattice",
+                                                                   "accept_p2l") if k in per_launch}
+        extras["roofline"] = {
+            "bound": "fp64", "kernel": top, "achieved": ach.get(top), "peak": peak64, "unit": "TFLOP/s",
+            "frac": (ach.get(top) / peak64) if ach.get(top) else None, "traffic": None,
+            "peak_source": "measured in this run: FP64 FMA issue rate (kmc_diag_fma_rate), not in "
+                           "MEASURED_PEAKS.json (HBM / bf16 only); these kernels are FP64-pipe bound",
+            "flops_per_launch": fm[top] if top in fm else None,
+            "per_kernel_ms": {k: round(v, 5) for k, v in per_launch.items()},
+            "per_kernel_tflops": {k: round(v, 4) for k, v in ach.items()},
+            "mean_neighbours_per_proposal": fm["mean_neighbours"]}
+
+        # e2e through the public API with host buffers
+        e2e_sys = LatticeHopSystem(side, OCC, seed=1 + rank)
+        st2 = make_state(e2e_sys.positions(), e2e_sys.charges(), e2e_sys.extent)
+        k2 = KMCFMM(st2.P, st2.Q, st2.domain, r=R, l=L, boundary_condition="pbc", max_move=1.0)
+        k2.initialise()
+        rng = np.random.default_rng(7)
+        for _ in range(2):
+            e2e_sys.step(k2, rng, BETA)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        n2 = 0
+        for _ in range(args.e2e_steps):
+            _, m2, _ = e2e_sys.proposals()
+            n2 += int(m2.sum())
+            e2e_sys.step(k2, rng, BETA)
+        torch.cuda.synchronize()
+        e2e_dt = time.perf_counter() - t0
+        n = e2e_sys.n
+        h2d = 8 + n * 8 + n * 18 * 8 + n * 6 * 8 + n * 6 * 8
+        d2h = n * 6 * 8 + 16
+        extras["e2e"] = {"value": n2 / e2e_dt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+        if rank == 0:
+            cores = os.cpu_count()
+            v, dt, npc = cpu_reference(args.cpu_steps, 1, side, None)
+            extras["cpu_baseline"] = {
+                "value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                "sample": f"{args.cpu_steps} KMC steps ({npc} proposals) of the same workload on the oracle "
+                          f"(restated reference CPU path, OpenMP {cores} threads; initial expansions zero, "
+                          f"which does not change the operation count)"}
+        k2.free()
+    kmc.free()
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": dict(workload_config(side, args.precision), proposals_per_step=nprop / args.steps,
+                               replicas=world),
+                "p50_ms": float(np.percentile(per_step, 50)), "p99_ms": float(np.percentile(per_step, 99)),
+                "clocks": clk, "gpu_launches": int(launches), "init_s": init_s}
+        line.update(extras)
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()
