@@ -97,7 +97,7 @@ def lib():
     return _lib
 
 
-NKERNELS = 11
+NKERNELS = 15
 
 
 def check(rc, what):
