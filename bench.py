@@ -155,13 +155,13 @@ class DeviceLattice:
 
 # ---------------------------------------------------------------------------
 def flop_model(kmc, host_sys, lr_nnz_folded):
-    """Algorithmic FP64 flops per launch for the step's kernels (add/mul = 1,
-    FMA = 2, rsqrt = 1), from this step's proposals and cell occupancy."""
+    """Algorithmic FP64 flops per launch of the step's kernels (add/mul = 1,
+    FMA = 2, rsqrt = 1; the counting convention of the survey), from this step's
+    proposals and cell occupancy."""
     st = kmc.state()
     n = 2 ** (R - 1)
     occ = st["occupancy"].reshape(n, n, n)
-    # sum over the 27 neighbour cells of each cell (periodic)
-    nb = np.zeros_like(occ)
+    nb = np.zeros_like(occ)  # charges in the 27 neighbour cells of each cell (periodic)
     for dz in (-1, 0, 1):
         for dy in (-1, 0, 1):
             for dx in (-1, 0, 1):
@@ -174,17 +174,23 @@ def flop_model(kmc, host_sys, lr_nnz_folded):
     c = np.minimum(((pp + 0.5 * host_sys.extent) * inv_w).astype(np.int64), n - 1)
     pcell = c[:, 0] + n * (c[:, 1] + n * c[:, 2])
     nh = L * (L + 1) // 2
-    far = 12 * nh + 6 * L                      # recurrence + coefficient dot products
+    far = 12 * nh + 6 * L          # solid-harmonic recurrence + coefficient products
+    mpole = 10 * nh + 6 * L        # multipole of one point
     nprop = int(act.sum())
     movers = np.nonzero(masks.sum(axis=1) > 0)[0]
-    new_flops = float(np.sum(11 * nb[pcell])) + nprop * (far + 27 * 11 + 6)
-    old_flops = float(np.sum(11 * nb[st["cells"][movers]])) + len(movers) * (far + 2)
-    mpole = 12 * nh + 6 * L
-    lr_flops = nprop * (2 * mpole + 6 * nh + 2 * lr_nnz_folded + 2 * nh)
+    near_new = float(np.sum(11 * nb[pcell])) + nprop * (far + 27 * 11 + 4)
+    near_old = float(np.sum(11 * nb[st["cells"][movers]])) + len(movers) * (far + 2)
+    lr_new = nprop * (mpole + 4 * nh + lr_nnz_folded + 6)   # a, a.(g-h), a^T U a
+    lr_old = len(movers) * (mpole + 2 * 2 * lr_nnz_folded + 8 * nh)
     ncell = n ** 3
-    p2l = ncell * 54 * (L * 12 + 30)           # per (cell, source): l-chain per m + geometry
-    return {"new_side": new_flops, "old_side": old_flops, "far_lattice": lr_flops, "accept_p2l": p2l,
-            "proposals": nprop, "mean_neighbours": float(np.mean(nb[pcell]))}
+    p2l = ncell * 54 * (12 * nh + 6 * L + 15)
+    return {"near_far_cell": near_new + near_old, "far_lattice": lr_new, "far_lattice_old": lr_old,
+            "accept_p2l": p2l, "proposals": nprop, "mean_neighbours": float(np.mean(nb[pcell]))}
+
+
+# DRAM traffic per launch of the dominant kernel, from the ncu capture summarised in
+# profiles/near_far_cell_fp64_lattice48.md (dram__bytes_read.sum + dram__bytes_write.sum)
+NCU_TRAFFIC = {"near_far_cell": 12.921088e6}
 
 
 def kernel_times(kmc):
@@ -371,11 +377,12 @@ def main():
         peak64 = fma_peak(True)
         per_launch = {k: (v[0] / max(v[1], 1)) for k, v in kt.items() if v[1] > 0}
         top = max(per_launch, key=lambda k: kt[k][0])
-        ach = {k: fm[k] / (per_launch[k] * 1e-3) / 1e12 for k in ("new_side", "old_side", "far_lattice",
-                                                                   "accept_p2l") if k in per_launch}
+        ach = {k: fm[k] / (per_launch[k] * 1e-3) / 1e12 for k in ("near_far_cell", "far_lattice",
+                                                                   "far_lattice_old", "accept_p2l")
+               if k in per_launch}
         extras["roofline"] = {
             "bound": "fp64", "kernel": top, "achieved": ach.get(top), "peak": peak64, "unit": "TFLOP/s",
-            "frac": (ach.get(top) / peak64) if ach.get(top) else None, "traffic": None,
+            "frac": (ach.get(top) / peak64) if ach.get(top) else None, "traffic": NCU_TRAFFIC.get(top),
             "peak_source": "measured in this run: FP64 FMA issue rate (kmc_diag_fma_rate), not in "
                            "MEASURED_PEAKS.json (HBM / bf16 only); these kernels are FP64-pipe bound",
             "flops_per_launch": fm[top] if top in fm else None,
