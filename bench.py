@@ -191,6 +191,7 @@ def flop_model(kmc, host_sys, lr_nnz_folded):
 # DRAM traffic per launch of the dominant kernel, from the ncu capture summarised in
 # profiles/near_far_cell_fp64_lattice48.md (dram__bytes_read.sum + dram__bytes_write.sum)
 NCU_TRAFFIC = {"near_far_cell": 12.921088e6}
+NCU_TRAFFIC_MIXED = {}
 
 
 def kernel_times(kmc):
@@ -279,13 +280,103 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------------------
+def make_system(side, rank, precision, local):
+    import torch
+    from coulomb_kmc_gb300 import KMCFMM
+    from coulomb_kmc_gb300.dats import make_state
+    from coulomb_kmc_gb300.workloads import LatticeHopSystem
+    hs = LatticeHopSystem(side, OCC, seed=1 + rank)
+    st = make_state(hs.positions(), hs.charges(), hs.extent)
+    kmc = KMCFMM(st.P, st.Q, st.domain, r=R, l=L, boundary_condition="pbc", max_move=1.0, precision=precision)
+    t0 = time.perf_counter()
+    kmc.initialise()
+    init_s = time.perf_counter() - t0
+    dev = DeviceLattice(hs, torch.device("cuda", local))
+    return hs, kmc, dev, init_s
+
+
+def timed_loop(kmc, dev, steps, warmup, flush, sampler=None):
+    import torch
+    for _ in range(warmup):
+        dev.step(kmc, BETA)
+    torch.cuda.synchronize()
+    kmc.check_errors()
+    kernel_times(kmc)  # reset counters
+    if sampler:
+        sampler.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    counts = []
+    torch.cuda.synchronize()
+    for i in range(steps):
+        flush.fill_(float(i))
+        ev[i][0].record()
+        dev.step(kmc, BETA)
+        ev[i][1].record()
+        counts.append(dev.masks.sum())
+    torch.cuda.synchronize()
+    clk = sampler.stop() if sampler else None
+    per_step = np.array([a.elapsed_time(b) for a, b in ev])
+    nprop = int(torch.stack(counts).sum().item())
+    _, launches = kernel_times(kmc)
+    kmc.check_errors()
+    return per_step, nprop, launches, clk
+
+
+def mixed_error_stats(side, local, nsteps=3):
+    """Mixed vs FP64 on identical states: relative dE error (denominator max(|dE|,1))
+    and Metropolis-decision agreement (u < exp(-beta dE) with shared u)."""
+    from coulomb_kmc_gb300 import KMCFMM
+    from coulomb_kmc_gb300.dats import make_state
+    from coulomb_kmc_gb300.workloads import LatticeHopSystem
+    hs = LatticeHopSystem(side, OCC, seed=11)
+    ks = {}
+    for prec in ("fp64", "mixed"):
+        st = make_state(hs.positions(), hs.charges(), hs.extent)
+        ks[prec] = KMCFMM(st.P, st.Q, st.domain, r=R, l=L, boundary_condition="pbc", max_move=1.0, precision=prec)
+        ks[prec].initialise()
+    rng = np.random.default_rng(5)
+    errs, agree, total, sel_agree = [], 0, 0, 0
+    for _ in range(nsteps):
+        ppos, masks, tsite = hs.proposals()
+        smc = np.array([6], np.int64)
+        sites = np.zeros((hs.n, 1), np.int64)
+        d = {}
+        for prec, k in ks.items():
+            d[prec] = np.zeros((hs.n, 6))
+            k.propose_with_dats(smc, sites, ppos, masks, d[prec])
+        act = masks > 0
+        a, b = d["mixed"][act], d["fp64"][act]
+        errs.append(np.abs(a - b) / np.maximum(np.abs(b), 1.0))
+        u = rng.uniform(size=a.shape)
+        agree += int(np.sum((u < np.exp(-BETA * a)) == (u < np.exp(-BETA * b))))
+        total += a.size
+        r1 = np.random.default_rng(total)
+        r2 = np.random.default_rng(total)
+        s1 = hs.select(d["mixed"], masks, r1, BETA)
+        s2 = hs.select(d["fp64"], masks, r2, BETA)
+        sel_agree += int(s1 == s2)
+        pid, h = s2
+        mv = ppos[pid, 3 * h:3 * h + 3].copy()
+        for k in ks.values():
+            k.accept((pid, mv))
+        hs.occ[hs.site_of[pid]] = -1
+        hs.occ[tsite[pid, h]] = pid
+        hs.site_of[pid] = tsite[pid, h]
+    e = np.concatenate(errs)
+    for k in ks.values():
+        k.free()
+    return {"max_rel": float(e.max()), "rms_rel": float(np.sqrt(np.mean(e * e))), "proposals": int(e.size),
+            "metropolis_decision_agreement": agree / total, "rejection_free_selection_agreement":
+                f"{sel_agree}/{nsteps}", "tolerance": 1e-6}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--side", type=int, default=SIDE)
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-steps", type=int, default=5)
@@ -306,48 +397,18 @@ def main():
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    from coulomb_kmc_gb300 import KMCFMM
+    from coulomb_kmc_gb300 import KMCFMM, _native
     from coulomb_kmc_gb300.dats import make_state
     from coulomb_kmc_gb300.workloads import LatticeHopSystem
 
     side = args.side
-    hs = LatticeHopSystem(side, OCC, seed=1 + rank)
-    st = make_state(hs.positions(), hs.charges(), hs.extent)
-    kmc = KMCFMM(st.P, st.Q, st.domain, r=R, l=L, boundary_condition="pbc", max_move=1.0)
-    t0 = time.perf_counter()
-    kmc.initialise()
-    init_s = time.perf_counter() - t0
-    dev = DeviceLattice(hs, torch.device("cuda", local))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-
-    for _ in range(args.warmup):
-        dev.step(kmc, BETA)
-    torch.cuda.synchronize()
-    kmc.check_errors()
-    from coulomb_kmc_gb300 import _native
-    kernel_times(kmc)  # reset counters
-    clocks = ClockSampler(local)
-    clocks.start()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    hs, kmc, dev, init_s = make_system(side, rank, args.precision, local)
     if world > 1:
         dist.barrier()
-    torch.cuda.synchronize()
-    nprop = 0
-    counts = []
-    for i in range(args.steps):
-        flush.fill_(float(i))
-        ev[i][0].record()
-        dev.step(kmc, BETA)
-        ev[i][1].record()
-        counts.append(dev.masks.sum())
-    torch.cuda.synchronize()
+    per_step, nprop, launches, clk = timed_loop(kmc, dev, args.steps, args.warmup, flush, ClockSampler(local))
     if world > 1:
         dist.barrier()
-    clk = clocks.stop()
-    per_step = np.array([a.elapsed_time(b) for a, b in ev])
-    nprop = int(torch.stack(counts).sum().item())
-    _, launches = kernel_times(kmc)
-    kmc.check_errors()
     t_ms = float(per_step.sum())
     tot = torch.tensor([t_ms, float(nprop)], dtype=torch.float64, device="cuda")
     if world > 1:
@@ -360,40 +421,59 @@ def main():
 
     extras = {}
     if not args.no_extras:
-        # per-kernel durations with CUDA events (separate pass so the timed loop is not perturbed)
+        # per-kernel durations with CUDA events (separate pass, the timed loop is not perturbed)
         _native.lib().kmc_profile(kmc._handle, 1)
         kernel_times(kmc)
-        host_snapshot = LatticeHopSystem(side, OCC, seed=1 + rank)
-        host_snapshot.site_of = dev.site_of.cpu().numpy()
-        host_snapshot.occ[:] = -1
-        host_snapshot.occ[host_snapshot.site_of] = np.arange(host_snapshot.n)
-        fm = flop_model(kmc, host_snapshot, folded_nnz())
-        prof_steps = 5
-        for i in range(prof_steps):
+        snap = LatticeHopSystem(side, OCC, seed=1 + rank)
+        snap.site_of = dev.site_of.cpu().numpy()
+        snap.occ[:] = -1
+        snap.occ[snap.site_of] = np.arange(snap.n)
+        fm = flop_model(kmc, snap, folded_nnz())
+        for i in range(5):
             flush.fill_(float(i))
             dev.step(kmc, BETA)
         kt, _ = kernel_times(kmc)
         _native.lib().kmc_profile(kmc._handle, 0)
-        peak64 = fma_peak(True)
+        peak64, peak32 = fma_peak(True), fma_peak(False)
         per_launch = {k: (v[0] / max(v[1], 1)) for k, v in kt.items() if v[1] > 0}
         top = max(per_launch, key=lambda k: kt[k][0])
         ach = {k: fm[k] / (per_launch[k] * 1e-3) / 1e12 for k in ("near_far_cell", "far_lattice",
                                                                    "far_lattice_old", "accept_p2l")
                if k in per_launch}
+        fp32_kernels = {"near_far_cell", "far_lattice"} if args.precision == "mixed" else set()
+        bound = "fp32" if top in fp32_kernels else "fp64"
+        peak = peak32 if bound == "fp32" else peak64
         extras["roofline"] = {
-            "bound": "fp64", "kernel": top, "achieved": ach.get(top), "peak": peak64, "unit": "TFLOP/s",
-            "frac": (ach.get(top) / peak64) if ach.get(top) else None, "traffic": NCU_TRAFFIC.get(top),
-            "peak_source": "measured in this run: FP64 FMA issue rate (kmc_diag_fma_rate), not in "
-                           "MEASURED_PEAKS.json (HBM / bf16 only); these kernels are FP64-pipe bound",
-            "flops_per_launch": fm[top] if top in fm else None,
+            "bound": bound, "kernel": top, "achieved": ach.get(top), "peak": peak, "unit": "TFLOP/s",
+            "frac": (ach.get(top) / peak) if ach.get(top) else None,
+            "traffic": NCU_TRAFFIC.get(top) if args.precision == "fp64" else NCU_TRAFFIC_MIXED.get(top),
+            "peak_source": "measured in this run with kmc_diag_fma_rate (FMA issue rate of the FP64 / FP32 "
+                           "pipe); MEASURED_PEAKS.json holds HBM and bf16 only, and these kernels are "
+                           "arithmetic bound with an L2-resident state",
+            "peaks_measured": {"fp64_tflops": peak64, "fp32_tflops": peak32},
+            "flops_convention": "algorithmic flops (add/mul 1, FMA 2, rsqrt 1) of the FP64 algorithm; "
+                                "the mixed kernels spend several FP32 instructions per algorithmic flop "
+                                "(double-FP32 pair terms)",
+            "flops_per_launch": fm.get(top),
             "per_kernel_ms": {k: round(v, 5) for k, v in per_launch.items()},
             "per_kernel_tflops": {k: round(v, 4) for k, v in ach.items()},
             "mean_neighbours_per_proposal": fm["mean_neighbours"]}
+        kmc.free()
+        # the plain FP64 path on the same workload, for the mixed/FP64 ratio
+        if args.precision == "mixed":
+            _, k64, d64, _ = make_system(side, rank, "fp64", local)
+            ps64, np64, _, _ = timed_loop(k64, d64, max(5, args.steps // 3), 2, flush)
+            extras["fp64"] = {"value": np64 / (ps64.sum() * 1e-3), "ms_per_step": float(ps64.mean()),
+                              "steps": len(ps64)}
+            extras["mixed_vs_fp64"] = value / extras["fp64"]["value"]
+            k64.free()
+            extras["mixed_error"] = mixed_error_stats(side, local)
 
         # e2e through the public API with host buffers
         e2e_sys = LatticeHopSystem(side, OCC, seed=1 + rank)
         st2 = make_state(e2e_sys.positions(), e2e_sys.charges(), e2e_sys.extent)
-        k2 = KMCFMM(st2.P, st2.Q, st2.domain, r=R, l=L, boundary_condition="pbc", max_move=1.0)
+        k2 = KMCFMM(st2.P, st2.Q, st2.domain, r=R, l=L, boundary_condition="pbc", max_move=1.0,
+                    precision=args.precision)
         k2.initialise()
         rng = np.random.default_rng(7)
         for _ in range(2):
@@ -411,6 +491,7 @@ def main():
         h2d = 8 + n * 8 + n * 18 * 8 + n * 6 * 8 + n * 6 * 8
         d2h = n * 6 * 8 + 16
         extras["e2e"] = {"value": n2 / e2e_dt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+        k2.free()
         if rank == 0:
             cores = os.cpu_count()
             v, dt, npc = cpu_reference(args.cpu_steps, 1, side, None)
@@ -419,12 +500,13 @@ def main():
                 "sample": f"{args.cpu_steps} KMC steps ({npc} proposals) of the same workload on the oracle "
                           f"(restated reference CPU path, OpenMP {cores} threads; initial expansions zero, "
                           f"which does not change the operation count)"}
-        k2.free()
-    kmc.free()
+    else:
+        kmc.free()
     if rank == 0:
+        dtype = "f64" if args.precision == "fp64" else "f32+df32 (f64 accept, energy, final difference)"
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
                 "config": dict(workload_config(side, args.precision), proposals_per_step=nprop / args.steps,
                                replicas=world),
                 "p50_ms": float(np.percentile(per_step, 50)), "p99_ms": float(np.percentile(per_step, 99)),

@@ -97,7 +97,7 @@ def lib():
     return _lib
 
 
-NKERNELS = 15
+NKERNELS = 16
 
 
 def check(rc, what):

@@ -1,0 +1,96 @@
+"""Mixed-precision propose path against the plain FP64 GPU path (same state):
+energy differences within 1e-6 relative (denominator max(|dE|,1)); the total
+energy and all expansions stay identical to the FP64 path through accepts."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import neutral_charges, rel_err
+from coulomb_kmc_gb300 import KMCFMM
+from coulomb_kmc_gb300.dats import make_state
+from coulomb_kmc_gb300.workloads import LatticeHopSystem
+
+pytestmark = pytest.mark.gpu
+MIXED_TOL = 1e-6
+
+
+def both(P, Q, E, bc, R, L, max_move=None):
+    out = []
+    for prec in ("fp64", "mixed"):
+        st = make_state(P, Q, E)
+        k = KMCFMM(st.P, st.Q, st.domain, r=R, l=L, boundary_condition=bc, max_move=max_move, precision=prec)
+        k.initialise()
+        out.append((k, st))
+    return out
+
+
+@pytest.mark.parametrize("bc", ["free_space", "27", "pbc"])
+@pytest.mark.parametrize("L", [8, 12])
+def test_mixed_offlattice(bc, L):
+    N, E, M = 400, 8.0, 4
+    rng = np.random.default_rng(3)
+    P = rng.uniform(-0.5 * E, 0.5 * E, (N, 3))
+    Q = neutral_charges(N)
+    (g64, _), (g32, _) = both(P, Q, E, bc, 3, L)
+    smc = np.array([M], np.int64)
+    sites = np.zeros((N, 1), np.int64)
+    masks = rng.integers(0, 2, (N, M)).astype(np.int64)
+    ppos = np.clip(np.repeat(P, M, axis=0).reshape(N, 3 * M) + rng.uniform(-0.5, 0.5, (N, 3 * M)),
+                   -0.5 * E, 0.5 * E)
+    d64, d32 = np.zeros((N, M)), np.zeros((N, M))
+    g64.propose_with_dats(smc, sites, ppos, masks, d64)
+    g32.propose_with_dats(smc, sites, ppos, masks, d32)
+    act = masks > 0
+    err = rel_err(d32[act], d64[act])
+    assert err.max() < MIXED_TOL, err.max()
+    assert np.array_equal(d32[~act], d64[~act])
+    g64.free()
+    g32.free()
+
+
+def test_mixed_lattice_and_accepts():
+    """pbc lattice hops: mixed differences within 1e-6; after accepting the same
+    moves the mixed instance's energy and state equal the FP64 instance's."""
+    hs = LatticeHopSystem(side=24, occupancy=0.25, seed=9)
+    (g64, s64), (g32, s32) = both(hs.positions(), hs.charges(), hs.extent, "pbc", 4, 12, max_move=1.0)
+    rng = np.random.default_rng(1)
+    worst = 0.0
+    for step in range(6):
+        ppos, masks, tsite = hs.proposals()
+        smc = np.array([6], np.int64)
+        sites = np.zeros((hs.n, 1), np.int64)
+        d64, d32 = np.zeros((hs.n, 6)), np.zeros((hs.n, 6))
+        g64.propose_with_dats(smc, sites, ppos, masks, d64)
+        g32.propose_with_dats(smc, sites, ppos, masks, d32)
+        act = masks > 0
+        worst = max(worst, rel_err(d32[act], d64[act]).max())
+        pid, h = hs.select(d64, masks, rng, 2.0)
+        mv = ppos[pid, 3 * h:3 * h + 3].copy()
+        g64.accept((pid, mv))
+        g32.accept((pid, mv))
+        hs.occ[hs.site_of[pid]] = -1
+        hs.occ[tsite[pid, h]] = pid
+        hs.site_of[pid] = tsite[pid, h]
+    assert worst < MIXED_TOL, worst
+    assert g32.energy == g64.energy
+    a, b = g32.state(), g64.state()
+    assert np.array_equal(a["local_expansions"], b["local_expansions"])
+    assert np.array_equal(a["occupancy"], b["occupancy"])
+    g64.free()
+    g32.free()
+
+
+def test_mixed_device_accept_energy_is_fp64():
+    """accept_device in mixed mode advances the energy by the FP64 difference."""
+    hs = LatticeHopSystem(side=16, occupancy=0.25, seed=4)
+    (g64, _), (g32, _) = both(hs.positions(), hs.charges(), hs.extent, "pbc", 3, 10, max_move=1.0)
+    ppos, masks, _ = hs.proposals()
+    pid = int(np.nonzero(masks.sum(axis=1))[0][0])
+    h = int(np.nonzero(masks[pid])[0][0])
+    mv = ppos[pid, 3 * h:3 * h + 3].copy()
+    d = torch.zeros(1, dtype=torch.float64, device="cuda")  # deliberately wrong dE: ignored in mixed mode
+    g32.accept_device(torch.tensor([pid], device="cuda"), torch.from_numpy(mv).cuda(), d)
+    g64.accept((pid, mv))
+    assert rel_err(g32.energy, g64.energy) < 1e-12
+    g64.free()
+    g32.free()
