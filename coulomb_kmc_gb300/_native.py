@@ -70,6 +70,7 @@ SIGNATURES = {
     "kmc_propose_moves": ([c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p], c_int),
     "kmc_accept": ([c_void_p, c_int64, POINTER(c_double)], c_int),
     "kmc_accept_device": ([c_void_p, c_void_p, c_void_p, c_void_p], c_int),
+    "kmc_propose_moves_noalloc": ([c_void_p, c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_void_p], c_int),
     "kmc_get_energy": ([c_void_p, POINTER(c_double)], c_int),
     "kmc_get_error": ([c_void_p, POINTER(c_int64), POINTER(c_int64)], c_int),
     "kmc_read_state": ([c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p], c_int),

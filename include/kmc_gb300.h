@@ -110,6 +110,24 @@ int kmc_accept(kmc_system *s, int64_t pid, const double new_position[3]);
 int kmc_accept_device(kmc_system *s, const int64_t *d_pid, const double *d_new_position,
                       const double *d_energy_diff);
 
+/* Allocation-free variant of kmc_propose_moves, for callers that must not
+ * allocate device memory during the call (for example code that runs while
+ * another component owns the allocator, or that is invoked from inside a
+ * stream capture region).  It has no counterpart in the reference.
+ * All pointers are device memory: particle ids d_pids[nump],
+ * d_exclusive_sum[nump+1] (proposal offsets), d_new_positions[total][3];
+ * d_diffs[total] receives dE * energy_unit, in proposal order.  FP64.
+ * Scratch is a fixed file-scope device array, not the handle's buffers:
+ * limits 4096 moving charges and 16384 proposals per call (larger calls
+ * return KMC_EINVAL with a message).  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture.  Every call on a device
+ * shares the array, so calls that overlap on the GPU (different streams or
+ * handles) race; serialise them.  Nothing in it needs clearing: each call
+ * writes every element it reads.  Does not synchronise. */
+int kmc_propose_moves_noalloc(kmc_system *s, int64_t nump, int64_t total, const int64_t *d_pids,
+                              const int64_t *d_exclusive_sum, const double *d_new_positions, double *d_diffs);
+
 /* Current total energy (synchronises). */
 int kmc_get_energy(kmc_system *s, double *energy_out);
 
