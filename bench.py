@@ -111,9 +111,7 @@ class DeviceLattice:
         self.smc = torch.tensor([6], dtype=torch.int64, device=device)
         self.sites = torch.zeros((self.n, 1), dtype=torch.int64, device=device)
         self.diffs = torch.zeros((self.n, self.M), dtype=torch.float64, device=device)
-        self.ar = torch.arange(self.n, device=device)
-        self.gen = torch.Generator(device=device)
-        self.gen.manual_seed(1234)
+        torch.cuda.manual_seed(1234)
 
     def build(self):
         t, k = self.t, self.k
@@ -129,7 +127,7 @@ class DeviceLattice:
         t = self.t
         rates = t.where(self.masks > 0, t.exp(-0.5 * beta * self.diffs), t.zeros_like(self.diffs)).reshape(-1)
         c = t.cumsum(rates, 0)
-        u = t.rand(1, generator=self.gen, device=c.device, dtype=t.float64) * c[-1]
+        u = t.rand(1, device=c.device, dtype=t.float64) * c[-1]
         idx = t.searchsorted(c, u, right=True).clamp_(max=c.numel() - 1)
         pid = idx // self.M
         h = idx % self.M
@@ -295,10 +293,36 @@ def make_system(side, rank, precision, local):
     return hs, kmc, dev, init_s
 
 
-def timed_loop(kmc, dev, steps, warmup, flush, sampler=None):
+def capture_step(kmc, dev, warmup):
+    """Warm up on a side stream, then capture one full KMC step in a CUDA graph.
+    Returns the graph and the number of library kernel launches per step."""
     import torch
-    for _ in range(warmup):
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(max(warmup, 2)):
+            dev.step(kmc, BETA)
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    kmc.check_errors()
+    _, l0 = kernel_times(kmc)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
         dev.step(kmc, BETA)
+    _, l1 = kernel_times(kmc)
+    return g, l1
+
+
+def timed_loop(kmc, dev, steps, warmup, flush, sampler=None, graph=True):
+    import torch
+    g, per_step_launches = None, None
+    if graph:
+        g, per_step_launches = capture_step(kmc, dev, warmup)
+        for _ in range(2):
+            g.replay()
+    else:
+        for _ in range(warmup):
+            dev.step(kmc, BETA)
     torch.cuda.synchronize()
     kmc.check_errors()
     kernel_times(kmc)  # reset counters
@@ -310,7 +334,10 @@ def timed_loop(kmc, dev, steps, warmup, flush, sampler=None):
     for i in range(steps):
         flush.fill_(float(i))
         ev[i][0].record()
-        dev.step(kmc, BETA)
+        if g is not None:
+            g.replay()
+        else:
+            dev.step(kmc, BETA)
         ev[i][1].record()
         counts.append(dev.masks.sum())
     torch.cuda.synchronize()
@@ -318,6 +345,8 @@ def timed_loop(kmc, dev, steps, warmup, flush, sampler=None):
     per_step = np.array([a.elapsed_time(b) for a, b in ev])
     nprop = int(torch.stack(counts).sum().item())
     _, launches = kernel_times(kmc)
+    if g is not None:
+        launches = per_step_launches * steps
     kmc.check_errors()
     return per_step, nprop, launches, clk
 
@@ -382,6 +411,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=5)
     ap.add_argument("--ref-steps", type=int, default=10)
     ap.add_argument("--no-extras", action="store_true", help="timed loop only (for profiler runs)")
+    ap.add_argument("--no-graph", action="store_true", help="launch the step eagerly instead of a CUDA graph")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
 
@@ -406,7 +436,8 @@ def main():
     hs, kmc, dev, init_s = make_system(side, rank, args.precision, local)
     if world > 1:
         dist.barrier()
-    per_step, nprop, launches, clk = timed_loop(kmc, dev, args.steps, args.warmup, flush, ClockSampler(local))
+    per_step, nprop, launches, clk = timed_loop(kmc, dev, args.steps, args.warmup, flush, ClockSampler(local),
+                                                graph=not args.no_graph)
     if world > 1:
         dist.barrier()
     t_ms = float(per_step.sum())
@@ -462,7 +493,7 @@ def main():
         # the plain FP64 path on the same workload, for the mixed/FP64 ratio
         if args.precision == "mixed":
             _, k64, d64, _ = make_system(side, rank, "fp64", local)
-            ps64, np64, _, _ = timed_loop(k64, d64, max(5, args.steps // 3), 2, flush)
+            ps64, np64, _, _ = timed_loop(k64, d64, max(5, args.steps // 3), 2, flush, graph=not args.no_graph)
             extras["fp64"] = {"value": np64 / (ps64.sum() * 1e-3), "ms_per_step": float(ps64.mean()),
                               "steps": len(ps64)}
             extras["mixed_vs_fp64"] = value / extras["fp64"]["value"]
@@ -510,7 +541,8 @@ def main():
                 "config": dict(workload_config(side, args.precision), proposals_per_step=nprop / args.steps,
                                replicas=world),
                 "p50_ms": float(np.percentile(per_step, 50)), "p99_ms": float(np.percentile(per_step, 99)),
-                "clocks": clk, "gpu_launches": int(launches), "init_s": init_s}
+                "clocks": clk, "gpu_launches": int(launches), "init_s": init_s,
+                "cuda_graph": not args.no_graph}
         line.update(extras)
         print(json.dumps(line))
     if world > 1:

@@ -98,7 +98,7 @@ def lib():
     return _lib
 
 
-NKERNELS = 16
+NKERNELS = 17
 
 
 def check(rc, what):
