@@ -137,10 +137,12 @@ class DeviceLattice:
         self.new_site = self.tsite[pid, h]
 
     def commit(self):
-        pid = self.d_pid
-        self.occ[self.site_of[pid]] = -1
-        self.occ[self.new_site] = pid
-        self.site_of[pid] = self.new_site
+        # device-only index updates (capturable in a CUDA graph)
+        pid = self.d_pid.view(-1)
+        ns = self.new_site.view(-1)
+        self.occ.index_fill_(0, self.site_of.index_select(0, pid), -1)
+        self.occ.index_copy_(0, ns, pid)
+        self.site_of.index_copy_(0, pid, ns)
 
     def step(self, kmc, beta):
         self.build()
