@@ -407,7 +407,7 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "mixed_fp64_accept", "fp64"])
     ap.add_argument("--side", type=int, default=SIDE)
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-steps", type=int, default=5)
@@ -500,6 +500,13 @@ def main():
                               "steps": len(ps64)}
             extras["mixed_vs_fp64"] = value / extras["fp64"]["value"]
             k64.free()
+            # mixed propose with the accept contributions kept in FP64
+            _, kmf, dmf, _ = make_system(side, rank, "mixed_fp64_accept", local)
+            psm, npm, _, _ = timed_loop(kmf, dmf, max(5, args.steps // 3), 2, flush, graph=not args.no_graph)
+            extras["mixed_fp64_accept"] = {"value": npm / (psm.sum() * 1e-3), "ms_per_step": float(psm.mean()),
+                                           "steps": len(psm),
+                                           "vs_fp64": (npm / (psm.sum() * 1e-3)) / extras["fp64"]["value"]}
+            kmf.free()
             extras["mixed_error"] = mixed_error_stats(side, local)
 
         # e2e through the public API with host buffers
@@ -536,7 +543,10 @@ def main():
     else:
         kmc.free()
     if rank == 0:
-        dtype = "f64" if args.precision == "fp64" else "f32+df32 (f64 accept, energy, final difference)"
+        dtype = {"fp64": "f64",
+                 "mixed": "f32+df32 (f64 master state, energy, lattice operator, final difference)",
+                 "mixed_fp64_accept": "f32+df32 (f64 accept, energy, lattice operator, final difference)"}[
+            args.precision]
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",

@@ -18,7 +18,7 @@ DEPS = SOURCES + [os.path.join(_PKG, "csrc", "kmc_sph.cuh"), os.path.join(_ROOT,
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 KMC_BC = {"free_space": 0, "27": 1, "pbc": 2}
-KMC_PREC = {"fp64": 0, "mixed": 1}
+KMC_PREC = {"fp64": 0, "mixed": 1, "mixed_fp64_accept": 2}
 KMC_ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "not initialised", -4: "bad proposed move",
               -5: "cell store overflow", -6: "out of memory"}
 

@@ -27,6 +27,10 @@
 __constant__ double c_rec_a[KMC_LMAX * KMC_LMAX];
 __constant__ double c_rec_b[KMC_LMAX * KMC_LMAX];
 __constant__ double c_rec_d[KMC_LMAX];
+// the same coefficients as FP32 pairs (hi, lo) for double-FP32 arithmetic
+__constant__ float2 c_rec_a2[KMC_LMAX * KMC_LMAX];
+__constant__ float2 c_rec_b2[KMC_LMAX * KMC_LMAX];
+__constant__ float2 c_rec_d2[KMC_LMAX];
 
 __host__ __device__ inline int hidx(int l, int m) { return (l * (l + 1)) / 2 + m; }
 

@@ -26,7 +26,13 @@ extern "C" {
 
 /* arithmetic of the propose path */
 #define KMC_PREC_FP64 0  /* plain FP64 drop-in */
-#define KMC_PREC_MIXED 1 /* FP32 near field / expansion evaluation over FP32 copies */
+/* Mixed precision (propose_with_dats): near field, expansion evaluation, self
+ * term and per-proposal lattice term in FP32 / double-FP32 over FP32 copies of
+ * the FP64 state; FP64 for the lattice operator applied to the multipole, the
+ * final old-minus-new difference and the total energy (the accepted move's
+ * difference is recomputed in FP64).  pbc: l <= 20. */
+#define KMC_PREC_MIXED 1             /* accept contributions in double-FP32, added to the FP64 master in FP64 */
+#define KMC_PREC_MIXED_FP64_ACCEPT 2 /* accept contributions in FP64 */
 
 #define KMC_OK 0
 #define KMC_EINVAL -1     /* bad argument */
