@@ -98,7 +98,7 @@ def lib():
     return _lib
 
 
-NKERNELS = 17
+NKERNELS = 18
 
 
 def check(rc, what):

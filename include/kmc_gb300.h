@@ -157,7 +157,7 @@ int kmc_info(kmc_system *s, int64_t *ncell, int64_t *capacity, int64_t *n);
  * milliseconds and launch counts since the last reset, and the number of kernel
  * launches issued by this handle.  Counterpart of the reference's per-component
  * timers in the PROFILE dictionary (common.py:136-160, kmc_fmm.py:894-912). */
-#define KMC_NKERNELS 17
+#define KMC_NKERNELS 18
 int kmc_profile(kmc_system *s, int32_t enable);
 int kmc_profile_read(kmc_system *s, int32_t reset, double *ms_out, int64_t *count_out, int64_t *launches_out);
 const char *kmc_kernel_name(int32_t id);
