@@ -13,12 +13,14 @@ _PKG = os.path.dirname(os.path.abspath(__file__))
 _ROOT = os.path.dirname(_PKG)
 BUILD_DIR = os.path.join(_PKG, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libkmc_gb300.so")
-SOURCES = [os.path.join(_PKG, "csrc", "kmc_gb300.cu")]
-DEPS = SOURCES + [os.path.join(_PKG, "csrc", "kmc_sph.cuh"), os.path.join(_ROOT, "include", "kmc_gb300.h")]
+SOURCES = [os.path.join(_PKG, "csrc", "kmc_gb300.cu"), os.path.join(_PKG, "csrc", "kmc_driver.cu")]
+DEPS = SOURCES + [os.path.join(_PKG, "csrc", n) for n in ("kmc_sph.cuh", "kmc_df32.cuh", "kmc_internal.h")] + [
+    os.path.join(_ROOT, "include", "kmc_gb300.h")]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 KMC_BC = {"free_space": 0, "27": 1, "pbc": 2}
 KMC_PREC = {"fp64": 0, "mixed": 1, "mixed_fp64_accept": 2}
+KMC_INIT = {"auto": 0, "exact": 1, "fmm": 2}
 KMC_ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "not initialised", -4: "bad proposed move",
               -5: "cell store overflow", -6: "out of memory"}
 
@@ -28,8 +30,18 @@ class KmcParams(ctypes.Structure):
         ("boundary", c_int32), ("r", c_int32), ("l", c_int32), ("precision", c_int32),
         ("extent", c_double), ("max_move", c_double), ("energy_unit", c_double),
         ("lr_nnz", c_int64), ("lr_data", POINTER(c_double)), ("lr_indptr", POINTER(c_int64)),
-        ("lr_indices", POINTER(c_int64)), ("lr_dipole", c_double * 3),
+        ("lr_indices", POINTER(c_int64)), ("lr_dipole", c_double * 3), ("initial_solve", c_int32),
     ]
+
+
+class KmcDriverParams(ctypes.Structure):
+    _fields_ = [
+        ("kind", c_int32), ("lattice_side", c_int32), ("beta", c_double), ("step", c_double),
+        ("seed", ctypes.c_uint64), ("lattice_sites", POINTER(c_int64)), ("log_capacity", c_int64),
+    ]
+
+
+KMC_DRIVE = {"lattice": 0, "offlattice": 1}
 
 
 def _nvcc():
@@ -78,6 +90,16 @@ SIGNATURES = {
     "kmc_profile": ([c_void_p, c_int32], c_int),
     "kmc_profile_read": ([c_void_p, c_int32, c_void_p, c_void_p, POINTER(c_int64)], c_int),
     "kmc_kernel_name": ([c_int32], c_char_p),
+    "kmc_set_tuning": ([c_void_p, c_int32, c_int32], c_int),
+    "kmc_get_tuning": ([c_void_p, c_int32, POINTER(c_int32)], c_int),
+    "kmc_driver_create": ([c_void_p, POINTER(KmcDriverParams), POINTER(c_void_p)], c_int),
+    "kmc_driver_step": ([c_void_p, c_int64], c_int),
+    "kmc_driver_capture": ([c_void_p], c_int),
+    "kmc_driver_launch": ([c_void_p, c_int64, c_void_p], c_int),
+    "kmc_driver_counters": ([c_void_p, POINTER(c_int64), POINTER(c_int64)], c_int),
+    "kmc_driver_log": ([c_void_p, c_int64, c_void_p, c_void_p, c_void_p, POINTER(c_int64)], c_int),
+    "kmc_driver_sites": ([c_void_p, c_void_p], c_int),
+    "kmc_driver_free": ([c_void_p], c_int),
     "kmc_diag_fma_rate": ([c_int32, c_int32, POINTER(c_double)], c_int),
     "kmc_free": ([c_void_p], c_int),
     "kmc_last_error": ([], c_char_p),

@@ -67,6 +67,30 @@ __device__ __forceinline__ df32 df_mul_f(const df32 a, const float b)
     return df32{h, l};
 }
 
+// a*b - c*d with one renormalisation (both products error-free)
+__device__ __forceinline__ df32 df_fms(const df32 a, const df32 b, const df32 c, const df32 d)
+{
+    float p1, e1, p2, e2;
+    two_prod(a.hi, b.hi, p1, e1);
+    two_prod(c.hi, d.hi, p2, e2);
+    float s, e;
+    two_sum(p1, -p2, s, e);
+    e += e1 - e2;
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    e = fmaf(-c.hi, d.lo, e);
+    e = fmaf(-c.lo, d.hi, e);
+    float h, l;
+    two_sum(s, e, h, l);
+    return df32{h, l};
+}
+
+// a*b + c*d
+__device__ __forceinline__ df32 df_fma2(const df32 a, const df32 b, const df32 c, const df32 d)
+{
+    return df_fms(a, b, df32{-c.hi, -c.lo}, d);
+}
+
 // acc += x without renormalising lo every step (accumulator form)
 __device__ __forceinline__ void df_acc(df32 &acc, const df32 x)
 {

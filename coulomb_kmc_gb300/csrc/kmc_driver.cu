@@ -1,0 +1,612 @@
+// Device-side KMC driver around one kmc_system: proposal generation,
+// selection and lattice occupancy on the GPU, so that a full KMC step
+// (generate -> propose_with_dats -> select -> accept) runs without a host
+// round trip and can be captured as one CUDA graph.
+//
+// It replaces the host bookkeeping of the reference's example driver
+// (examples/propose_with_dats_example.py:218-446: hop proposals to the six
+// nearest-neighbour sites, occupied-site masks, rates exp(-beta dE / 2),
+// cumulative-sum selection) and the Metropolis loops of its tests
+// (tests/host/test_free_space_1.py).
+//
+// Random numbers: Philox4x32-10 keyed by the seed; counter words
+// (step low, step high, index, attempt << 4 | tag), so every draw is a pure
+// function of (seed, step, index) and independent of launch shapes.
+#include "kmc_gb300.h"
+#include "kmc_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <new>
+#include <vector>
+
+namespace {
+
+constexpr int kGenThreads = 128;
+constexpr int kSelThreads = 256;                      // rate partial sums: threads per block
+constexpr int kSelItems = 4;                          // entries per thread
+constexpr int kSelChunk = kSelThreads * kSelItems;    // entries per partial sum
+constexpr int kPickThreads = kSelChunk;               // one entry per thread in the final pick
+constexpr int kMaxAttempts = 32;                      // re-draws of an off-lattice move that left the box
+
+enum { TAG_DISP_XY = 1, TAG_DISP_Z = 2, TAG_SELECT = 3 };
+
+struct P4 {
+    uint32_t v[4];
+};
+
+// Philox4x32-10 (Salmon, Moraes, Dror and Shaw, "Parallel random numbers: as
+// easy as 1, 2, 3", SC11): ten rounds, each two 32x32->64-bit products of the
+// counter words 0 and 2 with the published multipliers, the key bumped by the
+// published Weyl constants between rounds.
+__host__ __device__ inline P4 philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1)
+{
+    for (int r = 0; r < 10; ++r) {
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+        const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        c1 = (uint32_t)p1;
+        c3 = (uint32_t)p0;
+        c0 = n0;
+        c2 = n2;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return P4{{c0, c1, c2, c3}};
+}
+
+// uniform in [0, 1) with 53 random bits
+__host__ __device__ inline double u53(const uint32_t a, const uint32_t b)
+{
+    return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
+}
+
+struct Key {
+    uint32_t k0, k1;
+};
+
+__device__ __forceinline__ P4 draw(const Key k, const long long step, const uint32_t index, const uint32_t word3)
+{
+    return philox((uint32_t)step, (uint32_t)((unsigned long long)step >> 32), index, word3, k.k0, k.k1);
+}
+
+// ---------------------------------------------------------------------------
+// proposal generation
+// ---------------------------------------------------------------------------
+// hop order +x, -x, +y, -y, +z, -z (examples/propose_with_dats_example.py:265-290);
+// periodic systems wrap, a free-space lattice masks hops that leave it
+__global__ void k_lat_gen(const int N, const int side, const double spacing, const double half_e, const int wrap,
+                          const int *__restrict__ site_of, const int *__restrict__ occ, double *ppos,
+                          long long *masks, int *tsite)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const int s = site_of[i];
+    const int x = s % side, y = (s / side) % side, z = s / (side * side);
+    for (int h = 0; h < 6; ++h) {
+        int t[3] = {x, y, z};
+        const int ax = h >> 1, dir = (h & 1) ? -1 : 1;
+        t[ax] += dir;
+        bool ok = true;
+        if (t[ax] < 0 || t[ax] >= side) {
+            if (wrap)
+                t[ax] = (t[ax] + side) % side;
+            else
+                ok = false;
+        }
+        const int ts = ok ? t[0] + side * (t[1] + side * t[2]) : s;
+        tsite[6 * (size_t)i + h] = ts;
+        masks[6 * (size_t)i + h] = (ok && occ[ts] < 0) ? 1 : 0;
+        const int tx = ts % side, ty = (ts / side) % side, tz = ts / (side * side);
+        double *o = ppos + 18 * (size_t)i + 3 * h;
+        // explicit roundings (no contraction) so that host code reproduces the positions bit for bit
+        o[0] = __dadd_rn(__dsub_rn(__dmul_rn((double)tx, spacing), half_e), __dmul_rn(0.5, spacing));
+        o[1] = __dadd_rn(__dsub_rn(__dmul_rn((double)ty, spacing), half_e), __dmul_rn(0.5, spacing));
+        o[2] = __dadd_rn(__dsub_rn(__dmul_rn((double)tz, spacing), half_e), __dmul_rn(0.5, spacing));
+    }
+}
+
+// one displacement uniform in [-step, step]^3 per charge, re-drawn while it
+// leaves the box (at most kMaxAttempts draws, else a null move)
+__global__ void k_off_gen(const int N, const double half_e, const double step, const double *__restrict__ pos,
+                          const Key key, const long long *__restrict__ counters, double *ppos)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const long long st = counters[0];
+    const double x0 = pos[3 * (size_t)i], y0 = pos[3 * (size_t)i + 1], z0 = pos[3 * (size_t)i + 2];
+    double nx = x0, ny = y0, nz = z0;
+    for (int a = 0; a < kMaxAttempts; ++a) {
+        const P4 A = draw(key, st, (uint32_t)i, ((uint32_t)a << 4) | TAG_DISP_XY);
+        const P4 B = draw(key, st, (uint32_t)i, ((uint32_t)a << 4) | TAG_DISP_Z);
+        // x0 + (2u - 1) step with explicit roundings (reproducible on the host)
+        const double tx = __dadd_rn(x0, __dmul_rn(__dsub_rn(__dmul_rn(2.0, u53(A.v[0], A.v[1])), 1.0), step));
+        const double ty = __dadd_rn(y0, __dmul_rn(__dsub_rn(__dmul_rn(2.0, u53(A.v[2], A.v[3])), 1.0), step));
+        const double tz = __dadd_rn(z0, __dmul_rn(__dsub_rn(__dmul_rn(2.0, u53(B.v[0], B.v[1])), 1.0), step));
+        if (fabs(tx) <= half_e && fabs(ty) <= half_e && fabs(tz) <= half_e) {
+            nx = tx;
+            ny = ty;
+            nz = tz;
+            break;
+        }
+    }
+    ppos[3 * (size_t)i] = nx;
+    ppos[3 * (size_t)i + 1] = ny;
+    ppos[3 * (size_t)i + 2] = nz;
+}
+
+__global__ void k_fill_i64(long long *p, const long long n, const long long v)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+
+// ---------------------------------------------------------------------------
+// rejection-free selection: rate_e = exp(-beta dE_e / 2) on unmasked entries,
+// pick the first entry whose running sum exceeds u * total
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double rate_of(const long long e, const long long n, const double *diffs,
+                                          const long long *masks, const double hb)
+{
+    return (e < n && masks[e]) ? exp(-hb * diffs[e]) : 0.0;
+}
+
+__global__ void __launch_bounds__(kSelThreads) k_rate_partial(const long long n, const double *__restrict__ diffs,
+                                                              const long long *__restrict__ masks, const double hb,
+                                                              double *part)
+{
+    __shared__ double red[kSelThreads];
+    const long long base = (long long)blockIdx.x * kSelChunk + (long long)threadIdx.x * kSelItems;
+    double acc = 0.0;
+    for (int k = 0; k < kSelItems; ++k) acc += rate_of(base + k, n, diffs, masks, hb);
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = kSelThreads / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// inclusive scan of v[0..kPickThreads) in place (Hillis-Steele, fixed order)
+__device__ void block_scan(double *v)
+{
+    for (int off = 1; off < kPickThreads; off <<= 1) {
+        const double a = ((int)threadIdx.x >= off) ? v[threadIdx.x - off] : 0.0;
+        __syncthreads();
+        v[threadIdx.x] += a;
+        __syncthreads();
+    }
+}
+
+struct SelOut {
+    long long *pid;     // [1]
+    double *pos;        // [3]
+    double *de;         // [1]
+    long long *counters;  // [0] steps, [1] accepted
+    long long *log_pid, *log_tgt;
+    double *log_de;
+    long long log_cap;
+};
+
+__device__ void log_step(const SelOut &o, const long long st, const long long pid, const long long tgt, const double de)
+{
+    if (o.log_cap > 0) {
+        const long long k = st % o.log_cap;
+        o.log_pid[k] = pid;
+        o.log_tgt[k] = tgt;
+        o.log_de[k] = de;
+    }
+}
+
+__global__ void __launch_bounds__(kPickThreads) k_rate_pick(const long long n, const int nb, const int M,
+                                                            const double *__restrict__ diffs,
+                                                            const long long *__restrict__ masks, const double hb,
+                                                            const double *__restrict__ part,
+                                                            const double *__restrict__ ppos, const Key key,
+                                                            SelOut o, int *site_of, int *occ,
+                                                            const int *__restrict__ tsite)
+{
+    __shared__ double sc[kPickThreads];
+    __shared__ double s_target, s_base;
+    __shared__ int s_blk, s_first, s_last;
+    const int t = threadIdx.x;
+    const long long st = o.counters[0];
+    // runs of partial sums, one contiguous run per thread
+    const int per = (nb + kPickThreads - 1) / kPickThreads;
+    const int b0 = min(nb, t * per), b1 = min(nb, b0 + per);
+    double run = 0.0;
+    for (int b = b0; b < b1; ++b) run += part[b];
+    sc[t] = run;
+    if (t == 0) {
+        s_blk = -1;
+        s_first = 0x7fffffff;
+        s_last = -1;
+    }
+    __syncthreads();
+    block_scan(sc);
+    const double total = sc[kPickThreads - 1];
+    if (t == 0) {
+        const P4 r = draw(key, st, 0u, TAG_SELECT);
+        s_target = __dmul_rn(u53(r.v[0], r.v[1]), total);
+    }
+    __syncthreads();
+    const double target = s_target;
+    {
+        const double excl = t ? sc[t - 1] : 0.0;
+        if (b1 > b0 && excl <= target && target < sc[t]) {
+            double acc = excl;
+            for (int b = b0; b < b1; ++b) {
+                if (acc + part[b] > target && part[b] > 0.0) {
+                    s_blk = b;
+                    s_base = acc;
+                    break;
+                }
+                acc += part[b];
+            }
+        }
+    }
+    __syncthreads();
+    if (s_blk < 0 && t == 0) {
+        // target at or beyond the rounded total: the last block with a non-zero rate
+        double acc = 0.0;
+        for (int b = 0; b < nb; ++b) {
+            if (part[b] > 0.0) {
+                s_blk = b;
+                s_base = acc;
+            }
+            acc += part[b];
+        }
+        if (s_blk < 0) s_blk = 0;
+    }
+    __syncthreads();
+    const long long e = (long long)s_blk * kSelChunk + t;
+    const double r = rate_of(e, n, diffs, masks, hb);
+    __syncthreads();
+    sc[t] = r;
+    __syncthreads();
+    block_scan(sc);
+    if (r > 0.0 && s_base + sc[t] > target) atomicMin(&s_first, t);
+    if (r > 0.0) atomicMax(&s_last, t);
+    __syncthreads();
+    if (t == 0) {
+        const int pick = (s_first != 0x7fffffff) ? s_first : s_last;
+        if (pick < 0) {
+            // no unmasked proposal at all: no move this step
+            o.pid[0] = -1;
+            o.de[0] = 0.0;
+            log_step(o, st, -1, -1, 0.0);
+        } else {
+            const long long idx = (long long)s_blk * kSelChunk + pick;
+            const int pid = (int)(idx / M);
+            o.pid[0] = pid;
+            o.pos[0] = ppos[3 * idx];
+            o.pos[1] = ppos[3 * idx + 1];
+            o.pos[2] = ppos[3 * idx + 2];
+            o.de[0] = diffs[idx];
+            if (site_of) {
+                const int ns = tsite[idx];
+                occ[site_of[pid]] = -1;
+                occ[ns] = pid;
+                site_of[pid] = ns;
+                log_step(o, st, pid, ns, diffs[idx]);
+            } else {
+                log_step(o, st, pid, -1, diffs[idx]);
+            }
+            o.counters[1] += 1;
+        }
+        o.counters[0] = st + 1;
+    }
+}
+
+// Metropolis on one uniformly chosen charge: accept its proposal with
+// probability min(1, exp(-beta dE))
+__global__ void k_metropolis(const int N, const double beta, const double *__restrict__ diffs,
+                             const double *__restrict__ ppos, const Key key, SelOut o)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const long long st = o.counters[0];
+    const P4 r = draw(key, st, 0u, TAG_SELECT);
+    int i = (int)__dmul_rn(u53(r.v[0], r.v[1]), (double)N);
+    if (i >= N) i = N - 1;
+    const double de = diffs[i];
+    const bool acc = de <= 0.0 || u53(r.v[2], r.v[3]) < exp(-beta * de);
+    o.pid[0] = acc ? i : -1;
+    o.pos[0] = ppos[3 * (size_t)i];
+    o.pos[1] = ppos[3 * (size_t)i + 1];
+    o.pos[2] = ppos[3 * (size_t)i + 2];
+    o.de[0] = de;
+    log_step(o, st, acc ? i : -1, i, de);
+    if (acc) o.counters[1] += 1;
+    o.counters[0] = st + 1;
+}
+
+template <typename T>
+bool dmalloc(T **p, size_t n)
+{
+    return cudaMalloc((void **)p, sizeof(T) * (n ? n : 1)) == cudaSuccess;
+}
+
+} // namespace
+
+struct kmc_driver {
+    kmc_system *sys = nullptr;
+    kmc_driver_params prm{};
+    int N = 0, M = 1, side = 0, wrap = 0;
+    double E = 0.0, spacing = 1.0;
+    Key key{};
+    double *ppos = nullptr, *diffs = nullptr, *part = nullptr;
+    long long *masks = nullptr, *smc = nullptr, *sites = nullptr;
+    int *tsite = nullptr, *site_of = nullptr, *occ = nullptr;
+    long long *sel_pid = nullptr, *counters = nullptr, *log_pid = nullptr, *log_tgt = nullptr;
+    double *sel_pos = nullptr, *sel_de = nullptr, *log_de = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<void *> owned;
+};
+
+namespace {
+
+template <typename T>
+bool own(kmc_driver *d, T **p, size_t n)
+{
+    if (!dmalloc(p, n)) return false;
+    d->owned.push_back((void *)*p);
+    return true;
+}
+
+int enqueue_step(kmc_driver *d, cudaStream_t st)
+{
+    const int N = d->N;
+    const double half_e = 0.5 * d->E;
+    const unsigned gb = (unsigned)((N + kGenThreads - 1) / kGenThreads);
+    SelOut o{d->sel_pid, d->sel_pos, d->sel_de, d->counters, d->log_pid, d->log_tgt, d->log_de, d->prm.log_capacity};
+    if (d->prm.kind == KMC_DRIVE_LATTICE)
+        k_lat_gen<<<gb, kGenThreads, 0, st>>>(N, d->side, d->spacing, half_e, d->wrap, d->site_of, d->occ, d->ppos,
+                                              d->masks, d->tsite);
+    else
+        k_off_gen<<<gb, kGenThreads, 0, st>>>(N, half_e, d->prm.step, kmc_int_positions(d->sys), d->key,
+                                              d->counters, d->ppos);
+    if (cudaGetLastError() != cudaSuccess) return KMC_ECUDA;
+    int rc = kmc_propose_with_dats(d->sys, N, d->M, 1, (const int64_t *)d->smc, (const int64_t *)d->sites, d->ppos,
+                                   (const int64_t *)d->masks, nullptr, d->diffs);
+    if (rc) return rc;
+    if (d->prm.kind == KMC_DRIVE_LATTICE) {
+        const long long n = (long long)N * d->M;
+        const int nb = (int)((n + kSelChunk - 1) / kSelChunk);
+        const double hb = 0.5 * d->prm.beta;
+        k_rate_partial<<<nb, kSelThreads, 0, st>>>(n, d->diffs, d->masks, hb, d->part);
+        k_rate_pick<<<1, kPickThreads, 0, st>>>(n, nb, d->M, d->diffs, d->masks, hb, d->part, d->ppos, d->key, o,
+                                                d->site_of, d->occ, d->tsite);
+    } else {
+        k_metropolis<<<1, 32, 0, st>>>(N, d->prm.beta, d->diffs, d->ppos, d->key, o);
+    }
+    if (cudaGetLastError() != cudaSuccess) return KMC_ECUDA;
+    return kmc_accept_device(d->sys, (const int64_t *)d->sel_pid, d->sel_pos, d->sel_de);
+}
+
+void release(kmc_driver *d)
+{
+    if (d->exec) cudaGraphExecDestroy(d->exec);
+    if (d->graph) cudaGraphDestroy(d->graph);
+    for (void *p : d->owned) cudaFree(p);
+    delete d;
+}
+
+} // namespace
+
+int kmc_driver_create(kmc_system *s, const kmc_driver_params *p, kmc_driver **out)
+{
+    if (!s || !p || !out) return KMC_EINVAL;
+    *out = nullptr;
+    if (!kmc_int_initialised(s)) return KMC_ESTATE;
+    if ((p->kind != KMC_DRIVE_LATTICE && p->kind != KMC_DRIVE_OFFLATTICE) || !(p->beta >= 0.0) ||
+        p->log_capacity < 0)
+        return KMC_EINVAL;
+    const int N = kmc_int_n(s);
+    const double E = kmc_int_extent(s), max_move = kmc_int_max_move(s);
+    kmc_driver *d = new (std::nothrow) kmc_driver;
+    if (!d) return KMC_ENOMEM;
+    d->sys = s;
+    d->prm = *p;
+    d->prm.lattice_sites = nullptr;
+    d->N = N;
+    d->E = E;
+    d->key = Key{(uint32_t)p->seed, (uint32_t)(p->seed >> 32)};
+    cudaStream_t st = kmc_int_stream(s);
+    if (p->kind == KMC_DRIVE_LATTICE) {
+        if (p->lattice_side < 2 || !p->lattice_sites) {
+            delete d;
+            return KMC_EINVAL;
+        }
+        d->M = 6;
+        d->side = p->lattice_side;
+        d->spacing = E / p->lattice_side;
+        d->wrap = kmc_int_boundary(s) != KMC_BC_FREE_SPACE;
+        if (d->spacing > max_move) {
+            delete d;
+            return KMC_EINVAL;
+        }
+        // the charges must sit on the sites given; every site holds at most one
+        const long long nsites = (long long)d->side * d->side * d->side;
+        std::vector<int> occ((size_t)nsites, -1), so(N);
+        std::vector<double> pos(3 * (size_t)N);
+        if (cudaStreamSynchronize(st) != cudaSuccess ||
+            cudaMemcpy(pos.data(), kmc_int_positions(s), sizeof(double) * pos.size(), cudaMemcpyDeviceToHost) !=
+                cudaSuccess) {
+            delete d;
+            return KMC_ECUDA;
+        }
+        for (int i = 0; i < N; ++i) {
+            const long long site = p->lattice_sites[i];
+            if (site < 0 || site >= nsites || occ[(size_t)site] >= 0) {
+                delete d;
+                return KMC_EINVAL;
+            }
+            occ[(size_t)site] = i;
+            so[i] = (int)site;
+            const long long c[3] = {site % d->side, (site / d->side) % d->side, site / ((long long)d->side * d->side)};
+            for (int a = 0; a < 3; ++a) {
+                const double want = ((double)c[a] * d->spacing - 0.5 * E) + 0.5 * d->spacing;
+                if (fabs(pos[3 * (size_t)i + a] - want) > 1e-9 * (1.0 + fabs(E))) {
+                    delete d;
+                    return KMC_EINVAL;
+                }
+            }
+        }
+        if (!own(d, &d->site_of, N) || !own(d, &d->occ, (size_t)nsites) || !own(d, &d->tsite, 6 * (size_t)N)) {
+            release(d);
+            return KMC_ENOMEM;
+        }
+        if (cudaMemcpy(d->site_of, so.data(), sizeof(int) * N, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(d->occ, occ.data(), sizeof(int) * occ.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+            release(d);
+            return KMC_ECUDA;
+        }
+    } else {
+        if (!(p->step > 0.0) || p->step > max_move) {
+            delete d;
+            return KMC_EINVAL;
+        }
+        d->M = 1;
+    }
+    const size_t nm = (size_t)N * d->M;
+    const int nb = (int)((nm + kSelChunk - 1) / kSelChunk);
+    const size_t lc = (size_t)p->log_capacity;
+    if (!own(d, &d->ppos, 3 * nm) || !own(d, &d->diffs, nm) || !own(d, &d->masks, nm) || !own(d, &d->smc, 1) ||
+        !own(d, &d->sites, N) || !own(d, &d->part, nb) || !own(d, &d->sel_pid, 1) || !own(d, &d->sel_pos, 3) ||
+        !own(d, &d->sel_de, 1) || !own(d, &d->counters, 2) || !own(d, &d->log_pid, lc) || !own(d, &d->log_tgt, lc) ||
+        !own(d, &d->log_de, lc)) {
+        release(d);
+        return KMC_ENOMEM;
+    }
+    const long long smc = d->M;
+    bool ok = cudaMemcpy(d->smc, &smc, sizeof(long long), cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemset(d->sites, 0, sizeof(long long) * N) == cudaSuccess &&
+              cudaMemset(d->counters, 0, sizeof(long long) * 2) == cudaSuccess &&
+              cudaMemset(d->diffs, 0, sizeof(double) * nm) == cudaSuccess;
+    if (ok && p->kind == KMC_DRIVE_OFFLATTICE) {
+        k_fill_i64<<<(unsigned)((nm + 255) / 256), 256>>>(d->masks, (long long)nm, 1);
+        ok = cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess;
+    }
+    if (!ok) {
+        release(d);
+        return KMC_ECUDA;
+    }
+    int rc = kmc_int_reserve(s, N, (int64_t)nm);
+    if (rc) {
+        release(d);
+        return rc;
+    }
+    *out = d;
+    return KMC_OK;
+}
+
+int kmc_driver_step(kmc_driver *d, int64_t nsteps)
+{
+    if (!d || nsteps < 0) return KMC_EINVAL;
+    cudaStream_t st = kmc_int_stream(d->sys);
+    for (int64_t k = 0; k < nsteps; ++k) {
+        const int rc = enqueue_step(d, st);
+        if (rc) return rc;
+    }
+    return KMC_OK;
+}
+
+int kmc_driver_capture(kmc_driver *d)
+{
+    if (!d) return KMC_EINVAL;
+    cudaStream_t st = kmc_int_stream(d->sys);
+    if (!st) return KMC_EINVAL;  // the legacy default stream cannot be captured
+    if (d->exec) {
+        cudaGraphExecDestroy(d->exec);
+        d->exec = nullptr;
+    }
+    if (d->graph) {
+        cudaGraphDestroy(d->graph);
+        d->graph = nullptr;
+    }
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return KMC_ECUDA;
+    const int rc = enqueue_step(d, st);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (rc || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return rc ? rc : KMC_ECUDA;
+    }
+    d->graph = g;
+    if (cudaGraphInstantiate(&d->exec, g, 0) != cudaSuccess) return KMC_ECUDA;
+    return KMC_OK;
+}
+
+int kmc_driver_launch(kmc_driver *d, int64_t nsteps, void *stream)
+{
+    if (!d || nsteps < 0) return KMC_EINVAL;
+    if (!d->exec) return KMC_ESTATE;
+    cudaStream_t st = stream ? (cudaStream_t)stream : kmc_int_stream(d->sys);
+    for (int64_t k = 0; k < nsteps; ++k)
+        if (cudaGraphLaunch(d->exec, st) != cudaSuccess) return KMC_ECUDA;
+    return KMC_OK;
+}
+
+int kmc_driver_counters(kmc_driver *d, int64_t *steps_out, int64_t *accepted_out)
+{
+    if (!d) return KMC_EINVAL;
+    long long h[2];
+    if (cudaDeviceSynchronize() != cudaSuccess) return KMC_ECUDA;
+    if (cudaMemcpy(h, d->counters, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return KMC_ECUDA;
+    if (steps_out) *steps_out = h[0];
+    if (accepted_out) *accepted_out = h[1];
+    return KMC_OK;
+}
+
+int kmc_driver_log(kmc_driver *d, int64_t max_entries, int64_t *pid_out, int64_t *target_out, double *de_out,
+                   int64_t *n_out)
+{
+    if (!d || max_entries < 0 || !n_out) return KMC_EINVAL;
+    int64_t steps = 0;
+    int rc = kmc_driver_counters(d, &steps, nullptr);
+    if (rc) return rc;
+    const int64_t cap = d->prm.log_capacity;
+    const int64_t have = steps < cap ? steps : cap;
+    const int64_t n = have < max_entries ? have : max_entries;
+    std::vector<long long> a((size_t)cap), b((size_t)cap);
+    std::vector<double> c((size_t)cap);
+    if (cap > 0 && (cudaMemcpy(a.data(), d->log_pid, sizeof(long long) * cap, cudaMemcpyDeviceToHost) != cudaSuccess ||
+                    cudaMemcpy(b.data(), d->log_tgt, sizeof(long long) * cap, cudaMemcpyDeviceToHost) != cudaSuccess ||
+                    cudaMemcpy(c.data(), d->log_de, sizeof(double) * cap, cudaMemcpyDeviceToHost) != cudaSuccess))
+        return KMC_ECUDA;
+    const int64_t first = steps - have;  // oldest step still in the log
+    for (int64_t k = 0; k < n; ++k) {
+        const size_t j = (size_t)((first + k) % (cap ? cap : 1));
+        if (pid_out) pid_out[k] = a[j];
+        if (target_out) target_out[k] = b[j];
+        if (de_out) de_out[k] = c[j];
+    }
+    *n_out = n;
+    return KMC_OK;
+}
+
+int kmc_driver_sites(kmc_driver *d, int64_t *sites_out)
+{
+    if (!d || !sites_out) return KMC_EINVAL;
+    if (d->prm.kind != KMC_DRIVE_LATTICE) return KMC_EINVAL;
+    std::vector<int> so(d->N);
+    if (cudaDeviceSynchronize() != cudaSuccess) return KMC_ECUDA;
+    if (cudaMemcpy(so.data(), d->site_of, sizeof(int) * d->N, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return KMC_ECUDA;
+    for (int i = 0; i < d->N; ++i) sites_out[i] = so[i];
+    return KMC_OK;
+}
+
+int kmc_driver_free(kmc_driver *d)
+{
+    if (!d) return KMC_EINVAL;
+    cudaDeviceSynchronize();
+    release(d);
+    return KMC_OK;
+}

@@ -32,6 +32,15 @@ __constant__ float2 c_rec_a2[KMC_LMAX * KMC_LMAX];
 __constant__ float2 c_rec_b2[KMC_LMAX * KMC_LMAX];
 __constant__ float2 c_rec_d2[KMC_LMAX];
 
+// Scaled particle-to-local recurrence (accept path): with J_l^m = Ir_l^m / C_lm,
+//   C_mm = prod_{k<=m} d_k,  C_lm = a_lm C_{l-1,m},
+//   J_m^m = q r^{-1} ((x - i y)/r^2)^m,  J_l^m = (z/r^2) J_{l-1}^m - beta_lm r^{-2} J_{l-2}^m,
+//   beta_lm = b_lm / (a_lm a_{l-1,m})
+// so the recurrence needs one coefficient product per step; C_lm is applied once
+// per output in FP64.
+__constant__ float2 c_p2l_beta[KMC_LMAX * KMC_LMAX];
+__constant__ double c_p2l_scale[KMC_LMAX * KMC_LMAX];
+
 __host__ __device__ inline int hidx(int l, int m) { return (l * (l + 1)) / 2 + m; }
 
 // phi(x) = sum_{l<L} sum_{|m|<=l} Re(L_lm Rg_l^m(x)) for a folded expansion.

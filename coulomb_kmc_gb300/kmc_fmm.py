@@ -49,14 +49,18 @@ class KMCFMM:
     :arg l: number of expansion terms (default 12).
     :arg max_move: maximum per-axis displacement of a proposed move (default: box edge).
     :arg energy_unit: multiplies all energies.
-    :arg precision: 'fp64' (default, the drop-in).
+    :arg precision: 'fp64' (default, the drop-in), 'mixed' (FP32 / double-FP32 propose,
+        double-FP32 accept contributions added to the FP64 state) or 'mixed_fp64_accept'.
+    :arg initial_solve: 'auto' (default), 'exact' (direct particle-to-local sum) or 'fmm'
+        (octree P2M/M2M/M2L/L2L, the reference's method, kmc_fmm.py:956-959); 'auto' takes
+        the exact sum while cells x charges x images <= 1e9.
     ``shell_width``, ``_debug`` and ``cuda_direct`` are accepted for signature
     compatibility and have no effect (the whole path always runs on the GPU).
     """
 
     def __init__(self, positions, charges, domain, N=None, boundary_condition="pbc", r=None, shell_width=0.0,
                  energy_unit=1.0, _debug=False, l=None, max_move=None, cuda_direct=False, mirror_direction=None,
-                 precision="fp64"):
+                 precision="fp64", initial_solve="auto"):
         self._bc = BCType(boundary_condition)
         self.boundary_condition = self._bc
         if self._bc == BCType.FF_ONLY:
@@ -97,6 +101,9 @@ class KMCFMM:
         prm.extent = self.extent
         prm.max_move = self.max_move
         prm.energy_unit = self.energy_unit
+        if initial_solve not in _native.KMC_INIT:
+            raise ValueError("initial_solve must be one of %s" % sorted(_native.KMC_INIT))
+        prm.initial_solve = _native.KMC_INIT[initial_solve]
         if self._bc == BCType.PBC:
             data, indptr, indices, dip = lattice_operator(self.L, self.extent)
             self._lr = (data, indptr, indices, dip)

@@ -61,7 +61,15 @@ typedef struct kmc_params {
     const int64_t *lr_indptr;
     const int64_t *lr_indices;
     double lr_dipole[3];
+    /* how kmc_initialise builds the finest-level local expansions (KMC_INIT_*):
+       the reference runs ppmd's FMM (kmc_fmm.py:956-959); the exact particle-to-local
+       sum is the same quantity without the FMM truncation error */
+    int32_t initial_solve;
 } kmc_params;
+
+#define KMC_INIT_AUTO 0  /* exact below 1e9 (cells x charges x images), FMM above */
+#define KMC_INIT_EXACT 1 /* direct particle-to-local sum over all charges and images */
+#define KMC_INIT_FMM 2   /* P2M, M2M, M2L, L2L over the octree (FP64) */
 
 /* Create a system.  Replaces KMCFMM.__init__ (kmc_fmm.py:436-542) and the
  * component constructors it wires (FMMMPIDecomp, LocalParticleData,
@@ -161,6 +169,56 @@ int kmc_info(kmc_system *s, int64_t *ncell, int64_t *capacity, int64_t *n);
 int kmc_profile(kmc_system *s, int32_t enable);
 int kmc_profile_read(kmc_system *s, int32_t reset, double *ms_out, int64_t *count_out, int64_t *launches_out);
 const char *kmc_kernel_name(int32_t id);
+
+/* Launch-shape tuning (no reference counterpart; the reference has fixed
+ * OpenMP loops).  key: KMC_TUNE_*; value 0 restores the built-in choice.
+ * kmc_autotune times the candidates of every key on scratch buffers of this
+ * handle (the handle's state is not changed) and keeps the fastest. */
+#define KMC_TUNE_P2L_GROUPS 0 /* source groups per block of the double-FP32 accept kernel (1..4) */
+#define KMC_NTUNE 4
+int kmc_set_tuning(kmc_system *s, int32_t key, int32_t value);
+int kmc_get_tuning(kmc_system *s, int32_t key, int32_t *value_out);
+
+/* ------------------------------------------------------------------------
+ * Device-side KMC driver: proposal generation, selection and lattice
+ * occupancy on the GPU, so that a KMC step (generate, propose_with_dats,
+ * select, accept) needs no host round trip and can be captured as one CUDA
+ * graph.  Replaces the host bookkeeping of the reference's example driver
+ * (examples/propose_with_dats_example.py:218-446: hop proposals, occupied-site
+ * masks, rates exp(-beta dE / 2), cumulative-sum selection) and the Metropolis
+ * loops of its tests (tests/host/test_free_space_1.py).  Random numbers:
+ * Philox4x32-10 keyed by seed, counter (step, index, attempt, stream tag).
+ * ------------------------------------------------------------------------ */
+#define KMC_DRIVE_LATTICE 0    /* simple-cubic lattice hopping, rejection-free selection */
+#define KMC_DRIVE_OFFLATTICE 1 /* one uniform displacement per charge, Metropolis on one random charge */
+
+typedef struct kmc_driver kmc_driver;
+
+typedef struct kmc_driver_params {
+    int32_t kind;           /* KMC_DRIVE_* */
+    int32_t lattice_side;   /* lattice: sites per side (spacing extent / side, site i at -E/2 + (i + 1/2) spacing) */
+    double beta;            /* inverse temperature */
+    double step;            /* off-lattice: displacement uniform in [-step, step]^3, re-drawn if it leaves the box */
+    uint64_t seed;
+    const int64_t *lattice_sites; /* lattice: host array, site index of every charge (x fastest) */
+    int64_t log_capacity;   /* steps kept in the selection log (0: none) */
+} kmc_driver_params;
+
+int kmc_driver_create(kmc_system *s, const kmc_driver_params *p, kmc_driver **out);
+/* enqueue nsteps full KMC steps on the system's stream (no host synchronisation) */
+int kmc_driver_step(kmc_driver *d, int64_t nsteps);
+/* capture one step as a CUDA graph on the system's stream; kmc_driver_launch replays it */
+int kmc_driver_capture(kmc_driver *d);
+int kmc_driver_launch(kmc_driver *d, int64_t nsteps, void *stream);
+/* steps done, moves accepted (synchronises the system's stream) */
+int kmc_driver_counters(kmc_driver *d, int64_t *steps_out, int64_t *accepted_out);
+/* selection log, oldest first: particle id (-1 = rejected), target site (lattice) or -1,
+   energy difference of the selected proposal; n_out = entries written */
+int kmc_driver_log(kmc_driver *d, int64_t max_entries, int64_t *pid_out, int64_t *target_out, double *de_out,
+                   int64_t *n_out);
+/* lattice: site of every charge (host array of n) */
+int kmc_driver_sites(kmc_driver *d, int64_t *sites_out);
+int kmc_driver_free(kmc_driver *d);
 
 /* Diagnostic (no reference counterpart): measured FMA throughput of the
  * current device's FP64 (fp64 != 0) or FP32 pipe in TFLOP/s (FMA = 2 flops),
