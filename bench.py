@@ -8,16 +8,29 @@ proposals), all proposal energy differences are computed, one move is chosen
 with rate exp(-beta dE / 2), beta = 2, and accepted.
 
 Timed arms:
-  value : device resident -- proposals, masks, selection and bookkeeping on the
-          GPU (torch ops on device tensors) around the library's propose and
-          accept kernels; L2 flushed (256 MiB write) between timed steps.
+  value : device resident -- the library's device-side KMC driver (proposal
+          generation, rejection-free selection and occupancy kernels) around its
+          propose and accept kernels, one captured CUDA graph per step; L2 flushed
+          (256 MiB write) between timed steps.
   e2e   : the reference-facing API with host (numpy) buffers, exactly as the
           reference's driver uses it: host bookkeeping, propose_with_dats with
           host<->device copies, host selection, accept.
   --impl reference : the reference's CPU path as restated by the oracle
           (ppmd/coulomb_kmc cannot be built here), all host threads.
 
-Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Other workloads (--workload; each prints its own JSON line):
+  precision_split : 64^3 lattice, 65,536 charges, R=6, L in {8, 12, 16}: mixed vs
+                    FP64 error (max / RMS relative dE, Metropolis agreement) and
+                    throughput of both paths.
+  batched         : independent off-lattice systems (N log-uniform in
+                    [2,000, 131,072], half free_space, half pbc, density 0.25,
+                    L=12), one step of every system per round through one
+                    multi-stream launch of their captured step graphs; mixed vs FP64.
+  serving         : Poisson request stream through the continuous-batching
+                    server, p50/p99 round latency and throughput, against FP64
+                    one system at a time.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload ...]
 Multi-GPU (torchrun): independent replicas, one system per rank, no collective
 on the data path; value = proposals over all ranks / max rank time.
 """
@@ -91,68 +104,6 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-class DeviceLattice:
-    """Lattice-hop bookkeeping on the device (torch), feeding the library's
-    device-resident propose_with_dats / accept_device."""
-
-    def __init__(self, host_sys, device):
-        import torch
-        self.t = torch
-        self.k = host_sys.side
-        self.E = host_sys.extent
-        self.n = host_sys.n
-        self.M = 6
-        self.site_of = torch.from_numpy(host_sys.site_of.copy()).to(device)
-        occ = np.full(self.k ** 3, -1, np.int64)
-        occ[host_sys.site_of] = np.arange(self.n)
-        self.occ = torch.from_numpy(occ).to(device)
-        self.hops = torch.tensor([(1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)],
-                                 dtype=torch.int64, device=device)
-        self.smc = torch.tensor([6], dtype=torch.int64, device=device)
-        self.sites = torch.zeros((self.n, 1), dtype=torch.int64, device=device)
-        self.diffs = torch.zeros((self.n, self.M), dtype=torch.float64, device=device)
-        torch.cuda.manual_seed(1234)
-
-    def build(self):
-        t, k = self.t, self.k
-        s = self.site_of
-        xyz = torch_stack = t.stack((s % k, (s // k) % k, s // (k * k)), dim=1)
-        tgt = (torch_stack[:, None, :] + self.hops[None, :, :]) % k
-        self.tsite = tgt[..., 0] + k * (tgt[..., 1] + k * tgt[..., 2])
-        self.masks = (self.occ[self.tsite] < 0).to(t.int64)
-        self.ppos = (tgt.to(t.float64) - 0.5 * self.E + 0.5).reshape(self.n, 3 * self.M).contiguous()
-        del xyz
-
-    def select(self, beta):
-        t = self.t
-        rates = t.where(self.masks > 0, t.exp(-0.5 * beta * self.diffs), t.zeros_like(self.diffs)).reshape(-1)
-        c = t.cumsum(rates, 0)
-        u = t.rand(1, device=c.device, dtype=t.float64) * c[-1]
-        idx = t.searchsorted(c, u, right=True).clamp_(max=c.numel() - 1)
-        pid = idx // self.M
-        h = idx % self.M
-        self.d_pid = pid.contiguous()
-        self.d_new = self.ppos.view(self.n, self.M, 3)[pid, h].reshape(3).contiguous()
-        self.d_de = self.diffs.view(-1)[idx].contiguous()
-        self.new_site = self.tsite[pid, h]
-
-    def commit(self):
-        # device-only index updates (capturable in a CUDA graph)
-        pid = self.d_pid.view(-1)
-        ns = self.new_site.view(-1)
-        self.occ.index_fill_(0, self.site_of.index_select(0, pid), -1)
-        self.occ.index_copy_(0, ns, pid)
-        self.site_of.index_copy_(0, pid, ns)
-
-    def step(self, kmc, beta):
-        self.build()
-        kmc.propose_with_dats(self.smc, self.sites, self.ppos, self.masks, self.diffs, sync=False)
-        self.select(beta)
-        kmc.accept_device(self.d_pid, self.d_new, self.d_de)
-        self.commit()
-        return self.n
-
-
 # ---------------------------------------------------------------------------
 def flop_model(kmc, host_sys, lr_nnz_folded):
     """Algorithmic FP64 flops per launch of the step's kernels (add/mul = 1,
@@ -281,9 +232,9 @@ def run_reference(args):
 
 # ---------------------------------------------------------------------------
 def make_system(side, rank, precision, local):
-    import torch
     from coulomb_kmc_gb300 import KMCFMM
     from coulomb_kmc_gb300.dats import make_state
+    from coulomb_kmc_gb300.driver import KMCDriver
     from coulomb_kmc_gb300.workloads import LatticeHopSystem
     hs = LatticeHopSystem(side, OCC, seed=1 + rank)
     st = make_state(hs.positions(), hs.charges(), hs.extent)
@@ -291,75 +242,61 @@ def make_system(side, rank, precision, local):
     t0 = time.perf_counter()
     kmc.initialise()
     init_s = time.perf_counter() - t0
-    dev = DeviceLattice(hs, torch.device("cuda", local))
-    return hs, kmc, dev, init_s
+    drv = KMCDriver(kmc, "lattice", BETA, seed=1234 + rank, lattice_side=hs.side, lattice_sites=hs.site_of)
+    return hs, kmc, drv, init_s
 
 
-def capture_step(kmc, dev, warmup):
-    """Warm up on a side stream, then capture one full KMC step in a CUDA graph.
-    Returns the graph and the number of library kernel launches per step."""
+DRIVER_KERNELS_PER_STEP = 3  # proposal generation, rate partial sums, pick
+
+
+def timed_loop(kmc, drv, steps, warmup, flush, sampler=None, graph=True):
+    """Warm up, capture one KMC step (generate, propose, select, accept) as a CUDA
+    graph, then time `steps` replays with CUDA events on the driver's stream,
+    writing a 256 MiB buffer (L2 flush) before each timed step."""
     import torch
-    side = torch.cuda.Stream()
-    side.wait_stream(torch.cuda.current_stream())
-    with torch.cuda.stream(side):
-        for _ in range(max(warmup, 2)):
-            dev.step(kmc, BETA)
-    torch.cuda.current_stream().wait_stream(side)
+    drv.step(max(warmup, 1))
     torch.cuda.synchronize()
     kmc.check_errors()
     _, l0 = kernel_times(kmc)
-    g = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(g):
-        dev.step(kmc, BETA)
+    drv.step(1)
+    torch.cuda.synchronize()
     _, l1 = kernel_times(kmc)
-    return g, l1
-
-
-def timed_loop(kmc, dev, steps, warmup, flush, sampler=None, graph=True):
-    import torch
-    g, per_step_launches = None, None
+    per_step_launches = l1 + DRIVER_KERNELS_PER_STEP
     if graph:
-        g, per_step_launches = capture_step(kmc, dev, warmup)
-        for _ in range(2):
-            g.replay()
-    else:
-        for _ in range(warmup):
-            dev.step(kmc, BETA)
+        drv.capture()
+        drv.launch(2)
     torch.cuda.synchronize()
     kmc.check_errors()
-    kernel_times(kmc)  # reset counters
+    s0 = drv.stats()
     if sampler:
         sampler.start()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-    counts = []
     torch.cuda.synchronize()
-    for i in range(steps):
-        flush.fill_(float(i))
-        ev[i][0].record()
-        if g is not None:
-            g.replay()
-        else:
-            dev.step(kmc, BETA)
-        ev[i][1].record()
-        counts.append(dev.masks.sum())
+    with torch.cuda.stream(drv.stream):
+        for i in range(steps):
+            flush.fill_(float(i))
+            ev[i][0].record()
+            if graph:
+                drv.launch(1, stream=drv.stream)
+            else:
+                drv.step(1)
+            ev[i][1].record()
     torch.cuda.synchronize()
     clk = sampler.stop() if sampler else None
     per_step = np.array([a.elapsed_time(b) for a, b in ev])
-    nprop = int(torch.stack(counts).sum().item())
-    _, launches = kernel_times(kmc)
-    if g is not None:
-        launches = per_step_launches * steps
+    s1 = drv.stats()
+    nprop = s1[2] - s0[2]
     kmc.check_errors()
-    return per_step, nprop, launches, clk
+    return per_step, nprop, per_step_launches * steps, clk
 
 
-def mixed_error_stats(side, local, nsteps=3):
+def mixed_error_stats(side, local, nsteps=3, seed=11):
     """Mixed vs FP64 on identical states: relative dE error (denominator max(|dE|,1))
     and Metropolis-decision agreement (u < exp(-beta dE) with shared u)."""
     from coulomb_kmc_gb300 import KMCFMM
     from coulomb_kmc_gb300.dats import make_state
     from coulomb_kmc_gb300.workloads import LatticeHopSystem
-    hs = LatticeHopSystem(side, OCC, seed=11)
+    hs = LatticeHopSystem(side, OCC, seed=seed)
     ks = {}
     for prec in ("fp64", "mixed"):
         st = make_state(hs.positions(), hs.charges(), hs.extent)
@@ -401,6 +338,127 @@ def mixed_error_stats(side, local, nsteps=3):
                 f"{sel_agree}/{nsteps}", "tolerance": 1e-6}
 
 
+# ---------------------------------------------------------------------------
+def bench_precision_split(args):
+    """64^3 lattice, 65,536 charges (seed 2), R=6, L in {8, 12, 16}."""
+    import torch
+    side, r6 = 64, 6
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    out = {}
+    for Lx in args.orders:
+        res = {}
+        for prec in ("mixed", "fp64"):
+            from coulomb_kmc_gb300 import KMCFMM
+            from coulomb_kmc_gb300.dats import make_state
+            from coulomb_kmc_gb300.driver import KMCDriver
+            from coulomb_kmc_gb300.workloads import LatticeHopSystem
+            hs = LatticeHopSystem(side, OCC, seed=2)
+            st = make_state(hs.positions(), hs.charges(), hs.extent)
+            k = KMCFMM(st.P, st.Q, st.domain, r=r6, l=Lx, boundary_condition="pbc", max_move=1.0, precision=prec)
+            t0 = time.perf_counter()
+            k.initialise()
+            init_s = time.perf_counter() - t0
+            d = KMCDriver(k, "lattice", BETA, seed=99, lattice_side=side, lattice_sites=hs.site_of)
+            ps, npr, _, _ = timed_loop(k, d, args.steps, args.warmup, flush)
+            res[prec] = {"value": npr / (ps.sum() * 1e-3), "ms_per_step": float(ps.mean()), "init_s": init_s,
+                         "p99_ms": float(np.percentile(ps, 99))}
+            d.free()
+            k.free()
+        err = error_stats(side, r6, Lx, seed=2, nsteps=args.error_steps)
+        out[f"L{Lx}"] = {"mixed": res["mixed"], "fp64": res["fp64"],
+                         "mixed_vs_fp64": res["mixed"]["value"] / res["fp64"]["value"], "error": err}
+        print(json.dumps({"L": Lx, **out[f"L{Lx}"]}), file=sys.stderr)
+    line = {"metric": METRIC, "workload": "precision_split", "unit": UNIT,
+            "config": {"workload": "pbc lattice-hop 64^3 sites, 65,536 charges (seed 2), R=6, L swept",
+                       "orders": list(args.orders), "steps": args.steps, "warmup": args.warmup},
+            "results": out}
+    print(json.dumps(line))
+
+
+def error_stats(side, r, Lx, seed, nsteps):
+    """Mixed vs FP64 differences on identical states along an FP64-selected chain."""
+    global R, L
+    saved = (R, L)
+    R, L = r, Lx
+    try:
+        return mixed_error_stats(side, 0, nsteps=nsteps, seed=seed)
+    finally:
+        R, L = saved
+
+
+def bench_batched(args):
+    """Independent off-lattice systems advanced together, one step each per round."""
+    import torch
+    from coulomb_kmc_gb300.serving import Request, Server, Slot, build_system
+    rng = np.random.default_rng(3)
+    reqs = []
+    for i in range(args.systems):
+        n = int(round(np.exp(rng.uniform(np.log(2000), np.log(131072)))))
+        bc = "free_space" if i % 2 == 0 else "pbc"
+        reqs.append(Request(rid=i, kind="offlattice", bc=bc, n=n, rounds=args.rounds,
+                            seed=int(rng.integers(1, 2 ** 31)), L=12))
+    res = {}
+    for prec in ("mixed", "fp64"):
+        srv = Server(precision=prec, n_workers=args.workers)
+        t0 = time.perf_counter()
+        slots = []
+        for r in reqs:
+            k, d = build_system(r, prec)
+            slots.append(Slot(req=r, kmc=k, drv=d, nbytes=0, admitted=0.0))
+        build_s = time.perf_counter() - t0
+        for _ in range(2):
+            srv.round(slots)
+        s0 = sum(sl.drv.stats()[2] for sl in slots)
+        torch.cuda.synchronize()
+        ms = [srv.round(slots) for _ in range(args.rounds)]
+        s1 = sum(sl.drv.stats()[2] for sl in slots)
+        ms = np.array(ms)
+        res[prec] = {"value": (s1 - s0) / (ms.sum() * 1e-3), "round_ms_p50": float(np.percentile(ms, 50)),
+                     "round_ms_p99": float(np.percentile(ms, 99)), "build_s": build_s,
+                     "proposals_per_round": (s1 - s0) / len(ms)}
+        for sl in slots:
+            sl.drv.free()
+            sl.kmc.free()
+        print(json.dumps({prec: res[prec]}), file=sys.stderr)
+    line = {"metric": METRIC, "workload": "batched", "unit": UNIT, "value": res["mixed"]["value"],
+            "fp64": res["fp64"], "mixed": res["mixed"], "mixed_vs_fp64": res["mixed"]["value"] / res["fp64"]["value"],
+            "config": {"workload": f"{args.systems} independent off-lattice systems, N log-uniform in "
+                                   f"[2000, 131072] (seed 3), half free_space / half pbc, density 0.25, L=12, "
+                                   f"R=max(2, ceil(log8(N/8))), one proposal per charge per round, Metropolis "
+                                   f"beta=1", "rounds": args.rounds, "worker_streams": args.workers,
+                       "total_charges": int(sum(r.n for r in reqs))}}
+    print(json.dumps(line))
+
+
+def bench_serving(args):
+    """Poisson request stream through the continuous-batching server."""
+    from coulomb_kmc_gb300.serving import Server, one_at_a_time, poisson_requests
+    out = {}
+    for rate in args.rates:
+        reqs = poisson_requests(args.requests, rate, seed=4, n_range=(1000, args.max_n),
+                                k_range=(10, args.max_k))
+        srv = Server(precision="mixed", hbm_budget=150e9, max_active=args.max_active, n_workers=args.workers)
+        st = srv.serve(reqs, realtime=True)
+        st["peak_active"] = srv.peak_active
+        out[str(rate)] = st
+        print(json.dumps({"rate": rate, **st}), file=sys.stderr)
+    reqs = poisson_requests(args.requests, args.rates[0], seed=4, n_range=(1000, args.max_n),
+                            k_range=(10, args.max_k))
+    p64, s64 = one_at_a_time(reqs, "fp64")
+    base = p64 / s64
+    line = {"metric": METRIC, "workload": "serving", "unit": UNIT,
+            "value": max(v["proposals_per_s"] for v in out.values()),
+            "fp64_one_at_a_time": base,
+            "mixed_vs_fp64": max(v["proposals_per_s"] for v in out.values()) / base,
+            "per_rate": out,
+            "config": {"workload": f"{args.requests} requests (seed 4), Poisson arrivals, N log-uniform in "
+                                   f"[1000, {args.max_n}], lattice-hop pbc or off-lattice free_space with "
+                                   f"probability 1/2, L=12, K uniform in [10, {args.max_k}], 150 GB budget",
+                       "rates_per_s": list(args.rates), "max_active": args.max_active,
+                       "worker_streams": args.workers}}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -414,8 +472,25 @@ def main():
     ap.add_argument("--ref-steps", type=int, default=10)
     ap.add_argument("--no-extras", action="store_true", help="timed loop only (for profiler runs)")
     ap.add_argument("--no-graph", action="store_true", help="launch the step eagerly instead of a CUDA graph")
+    ap.add_argument("--workload", default="lattice48", choices=["lattice48", "precision_split", "batched", "serving"])
+    ap.add_argument("--orders", type=int, nargs="+", default=[8, 12, 16])
+    ap.add_argument("--error-steps", type=int, default=3)
+    ap.add_argument("--systems", type=int, default=64)
+    ap.add_argument("--rounds", type=int, default=20)
+    ap.add_argument("--workers", type=int, default=8)
+    ap.add_argument("--requests", type=int, default=48)
+    ap.add_argument("--rates", type=float, nargs="+", default=[50.0, 2000.0])
+    ap.add_argument("--max-n", type=int, default=262144)
+    ap.add_argument("--max-k", type=int, default=100)
+    ap.add_argument("--max-active", type=int, default=64)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
+    if args.workload != "lattice48" and args.impl == "ours":
+        import torch
+        torch.cuda.set_device(0)
+        {"precision_split": bench_precision_split, "batched": bench_batched, "serving": bench_serving}[
+            args.workload](args)
+        return
 
     if args.impl == "reference":
         run_reference(args)
@@ -435,10 +510,10 @@ def main():
 
     side = args.side
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    hs, kmc, dev, init_s = make_system(side, rank, args.precision, local)
+    hs, kmc, drv, init_s = make_system(side, rank, args.precision, local)
     if world > 1:
         dist.barrier()
-    per_step, nprop, launches, clk = timed_loop(kmc, dev, args.steps, args.warmup, flush, ClockSampler(local),
+    per_step, nprop, launches, clk = timed_loop(kmc, drv, args.steps, args.warmup, flush, ClockSampler(local),
                                                 graph=not args.no_graph)
     if world > 1:
         dist.barrier()
@@ -458,13 +533,13 @@ def main():
         _native.lib().kmc_profile(kmc._handle, 1)
         kernel_times(kmc)
         snap = LatticeHopSystem(side, OCC, seed=1 + rank)
-        snap.site_of = dev.site_of.cpu().numpy()
+        snap.site_of = drv.sites()
         snap.occ[:] = -1
         snap.occ[snap.site_of] = np.arange(snap.n)
         fm = flop_model(kmc, snap, folded_nnz())
         for i in range(5):
             flush.fill_(float(i))
-            dev.step(kmc, BETA)
+            drv.step(1)
         kt, _ = kernel_times(kmc)
         _native.lib().kmc_profile(kmc._handle, 0)
         peak64, peak32 = fma_peak(True), fma_peak(False)
@@ -491,11 +566,13 @@ def main():
             "per_kernel_ms": {k: round(v, 5) for k, v in per_launch.items()},
             "per_kernel_tflops": {k: round(v, 4) for k, v in ach.items()},
             "mean_neighbours_per_proposal": fm["mean_neighbours"]}
+        drv.free()
         kmc.free()
         # the plain FP64 path on the same workload, for the mixed/FP64 ratio
         if args.precision == "mixed":
             _, k64, d64, _ = make_system(side, rank, "fp64", local)
             ps64, np64, _, _ = timed_loop(k64, d64, max(5, args.steps // 3), 2, flush, graph=not args.no_graph)
+            d64.free()
             extras["fp64"] = {"value": np64 / (ps64.sum() * 1e-3), "ms_per_step": float(ps64.mean()),
                               "steps": len(ps64)}
             extras["mixed_vs_fp64"] = value / extras["fp64"]["value"]
@@ -503,6 +580,7 @@ def main():
             # mixed propose with the accept contributions kept in FP64
             _, kmf, dmf, _ = make_system(side, rank, "mixed_fp64_accept", local)
             psm, npm, _, _ = timed_loop(kmf, dmf, max(5, args.steps // 3), 2, flush, graph=not args.no_graph)
+            dmf.free()
             extras["mixed_fp64_accept"] = {"value": npm / (psm.sum() * 1e-3), "ms_per_step": float(psm.mean()),
                                            "steps": len(psm),
                                            "vs_fp64": (npm / (psm.sum() * 1e-3)) / extras["fp64"]["value"]}
@@ -541,6 +619,7 @@ def main():
                           f"(restated reference CPU path, OpenMP {cores} threads; initial expansions zero, "
                           f"which does not change the operation count)"}
     else:
+        drv.free()
         kmc.free()
     if rank == 0:
         dtype = {"fp64": "f64",

@@ -96,10 +96,11 @@ SIGNATURES = {
     "kmc_driver_step": ([c_void_p, c_int64], c_int),
     "kmc_driver_capture": ([c_void_p], c_int),
     "kmc_driver_launch": ([c_void_p, c_int64, c_void_p], c_int),
-    "kmc_driver_counters": ([c_void_p, POINTER(c_int64), POINTER(c_int64)], c_int),
+    "kmc_driver_counters": ([c_void_p, POINTER(c_int64), POINTER(c_int64), POINTER(c_int64)], c_int),
     "kmc_driver_log": ([c_void_p, c_int64, c_void_p, c_void_p, c_void_p, POINTER(c_int64)], c_int),
     "kmc_driver_sites": ([c_void_p, c_void_p], c_int),
     "kmc_driver_free": ([c_void_p], c_int),
+    "kmc_drivers_launch": ([c_void_p, c_int64, c_int64, c_void_p, c_void_p, c_int64], c_int),
     "kmc_diag_fma_rate": ([c_int32, c_int32, POINTER(c_double)], c_int),
     "kmc_free": ([c_void_p], c_int),
     "kmc_last_error": ([], c_char_p),

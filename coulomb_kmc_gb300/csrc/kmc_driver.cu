@@ -156,14 +156,23 @@ __device__ __forceinline__ double rate_of(const long long e, const long long n, 
 
 __global__ void __launch_bounds__(kSelThreads) k_rate_partial(const long long n, const double *__restrict__ diffs,
                                                               const long long *__restrict__ masks, const double hb,
-                                                              double *part)
+                                                              double *part, long long *counters)
 {
     __shared__ double red[kSelThreads];
+    __shared__ int active;
+    if (threadIdx.x == 0) active = 0;
+    __syncthreads();
     const long long base = (long long)blockIdx.x * kSelChunk + (long long)threadIdx.x * kSelItems;
     double acc = 0.0;
-    for (int k = 0; k < kSelItems; ++k) acc += rate_of(base + k, n, diffs, masks, hb);
+    int na = 0;
+    for (int k = 0; k < kSelItems; ++k) {
+        acc += rate_of(base + k, n, diffs, masks, hb);
+        na += (base + k < n && masks[base + k]) ? 1 : 0;
+    }
+    if (na) atomicAdd(&active, na);
     red[threadIdx.x] = acc;
     __syncthreads();
+    if (threadIdx.x == 0) atomicAdd((unsigned long long *)&counters[2], (unsigned long long)active);
     for (int w = kSelThreads / 2; w > 0; w >>= 1) {
         if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
         __syncthreads();
@@ -186,7 +195,7 @@ struct SelOut {
     long long *pid;     // [1]
     double *pos;        // [3]
     double *de;         // [1]
-    long long *counters;  // [0] steps, [1] accepted
+    long long *counters;  // [0] steps, [1] accepted, [2] proposals evaluated
     long long *log_pid, *log_tgt;
     double *log_de;
     long long log_cap;
@@ -321,6 +330,7 @@ __global__ void k_metropolis(const int N, const double beta, const double *__res
     o.de[0] = de;
     log_step(o, st, acc ? i : -1, i, de);
     if (acc) o.counters[1] += 1;
+    o.counters[2] += N;
     o.counters[0] = st + 1;
 }
 
@@ -378,7 +388,7 @@ int enqueue_step(kmc_driver *d, cudaStream_t st)
         const long long n = (long long)N * d->M;
         const int nb = (int)((n + kSelChunk - 1) / kSelChunk);
         const double hb = 0.5 * d->prm.beta;
-        k_rate_partial<<<nb, kSelThreads, 0, st>>>(n, d->diffs, d->masks, hb, d->part);
+        k_rate_partial<<<nb, kSelThreads, 0, st>>>(n, d->diffs, d->masks, hb, d->part, d->counters);
         k_rate_pick<<<1, kPickThreads, 0, st>>>(n, nb, d->M, d->diffs, d->masks, hb, d->part, d->ppos, d->key, o,
                                                 d->site_of, d->occ, d->tsite);
     } else {
@@ -478,7 +488,7 @@ int kmc_driver_create(kmc_system *s, const kmc_driver_params *p, kmc_driver **ou
     const size_t lc = (size_t)p->log_capacity;
     if (!own(d, &d->ppos, 3 * nm) || !own(d, &d->diffs, nm) || !own(d, &d->masks, nm) || !own(d, &d->smc, 1) ||
         !own(d, &d->sites, N) || !own(d, &d->part, nb) || !own(d, &d->sel_pid, 1) || !own(d, &d->sel_pos, 3) ||
-        !own(d, &d->sel_de, 1) || !own(d, &d->counters, 2) || !own(d, &d->log_pid, lc) || !own(d, &d->log_tgt, lc) ||
+        !own(d, &d->sel_de, 1) || !own(d, &d->counters, 3) || !own(d, &d->log_pid, lc) || !own(d, &d->log_tgt, lc) ||
         !own(d, &d->log_de, lc)) {
         release(d);
         return KMC_ENOMEM;
@@ -486,7 +496,7 @@ int kmc_driver_create(kmc_system *s, const kmc_driver_params *p, kmc_driver **ou
     const long long smc = d->M;
     bool ok = cudaMemcpy(d->smc, &smc, sizeof(long long), cudaMemcpyHostToDevice) == cudaSuccess &&
               cudaMemset(d->sites, 0, sizeof(long long) * N) == cudaSuccess &&
-              cudaMemset(d->counters, 0, sizeof(long long) * 2) == cudaSuccess &&
+              cudaMemset(d->counters, 0, sizeof(long long) * 3) == cudaSuccess &&
               cudaMemset(d->diffs, 0, sizeof(double) * nm) == cudaSuccess;
     if (ok && p->kind == KMC_DRIVE_OFFLATTICE) {
         k_fill_i64<<<(unsigned)((nm + 255) / 256), 256>>>(d->masks, (long long)nm, 1);
@@ -553,14 +563,15 @@ int kmc_driver_launch(kmc_driver *d, int64_t nsteps, void *stream)
     return KMC_OK;
 }
 
-int kmc_driver_counters(kmc_driver *d, int64_t *steps_out, int64_t *accepted_out)
+int kmc_driver_counters(kmc_driver *d, int64_t *steps_out, int64_t *accepted_out, int64_t *proposals_out)
 {
     if (!d) return KMC_EINVAL;
-    long long h[2];
-    if (cudaDeviceSynchronize() != cudaSuccess) return KMC_ECUDA;
+    long long h[3];
+    if (cudaStreamSynchronize(kmc_int_stream(d->sys)) != cudaSuccess) return KMC_ECUDA;
     if (cudaMemcpy(h, d->counters, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return KMC_ECUDA;
     if (steps_out) *steps_out = h[0];
     if (accepted_out) *accepted_out = h[1];
+    if (proposals_out) *proposals_out = h[2];
     return KMC_OK;
 }
 
@@ -569,7 +580,7 @@ int kmc_driver_log(kmc_driver *d, int64_t max_entries, int64_t *pid_out, int64_t
 {
     if (!d || max_entries < 0 || !n_out) return KMC_EINVAL;
     int64_t steps = 0;
-    int rc = kmc_driver_counters(d, &steps, nullptr);
+    int rc = kmc_driver_counters(d, &steps, nullptr, nullptr);
     if (rc) return rc;
     const int64_t cap = d->prm.log_capacity;
     const int64_t have = steps < cap ? steps : cap;
@@ -596,7 +607,7 @@ int kmc_driver_sites(kmc_driver *d, int64_t *sites_out)
     if (!d || !sites_out) return KMC_EINVAL;
     if (d->prm.kind != KMC_DRIVE_LATTICE) return KMC_EINVAL;
     std::vector<int> so(d->N);
-    if (cudaDeviceSynchronize() != cudaSuccess) return KMC_ECUDA;
+    if (cudaStreamSynchronize(kmc_int_stream(d->sys)) != cudaSuccess) return KMC_ECUDA;
     if (cudaMemcpy(so.data(), d->site_of, sizeof(int) * d->N, cudaMemcpyDeviceToHost) != cudaSuccess)
         return KMC_ECUDA;
     for (int i = 0; i < d->N; ++i) sites_out[i] = so[i];
@@ -606,7 +617,36 @@ int kmc_driver_sites(kmc_driver *d, int64_t *sites_out)
 int kmc_driver_free(kmc_driver *d)
 {
     if (!d) return KMC_EINVAL;
-    cudaDeviceSynchronize();
+    cudaStreamSynchronize(kmc_int_stream(d->sys));
     release(d);
+    return KMC_OK;
+}
+
+int kmc_drivers_launch(kmc_driver **drivers, int64_t n, int64_t steps, void *main_stream, void **worker_streams,
+                       int64_t n_workers)
+{
+    if (!drivers || n < 0 || steps < 0 || !worker_streams || n_workers <= 0) return KMC_EINVAL;
+    for (int64_t i = 0; i < n; ++i)
+        if (!drivers[i] || !drivers[i]->exec) return KMC_ESTATE;
+    // fork/join events, grown on demand and kept for the process
+    static std::vector<cudaEvent_t> ev;
+    while ((int64_t)ev.size() < n_workers + 1) {
+        cudaEvent_t e;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return KMC_ECUDA;
+        ev.push_back(e);
+    }
+    cudaStream_t ms = (cudaStream_t)main_stream;
+    if (cudaEventRecord(ev[0], ms) != cudaSuccess) return KMC_ECUDA;
+    const int64_t nw = n_workers < n ? n_workers : n;
+    for (int64_t w = 0; w < nw; ++w)
+        if (cudaStreamWaitEvent((cudaStream_t)worker_streams[w], ev[0], 0) != cudaSuccess) return KMC_ECUDA;
+    for (int64_t k = 0; k < steps; ++k)
+        for (int64_t i = 0; i < n; ++i)
+            if (cudaGraphLaunch(drivers[i]->exec, (cudaStream_t)worker_streams[i % nw]) != cudaSuccess)
+                return KMC_ECUDA;
+    for (int64_t w = 0; w < nw; ++w) {
+        if (cudaEventRecord(ev[w + 1], (cudaStream_t)worker_streams[w]) != cudaSuccess) return KMC_ECUDA;
+        if (cudaStreamWaitEvent(ms, ev[w + 1], 0) != cudaSuccess) return KMC_ECUDA;
+    }
     return KMC_OK;
 }

@@ -97,9 +97,14 @@ class KMCDriver:
 
     def counters(self):
         """(steps done, moves accepted); synchronises the device."""
-        a, b = c_int64(), c_int64()
-        _native.check(_native.lib().kmc_driver_counters(self._handle, byref(a), byref(b)), "kmc_driver_counters")
-        return a.value, b.value
+        return self.stats()[:2]
+
+    def stats(self):
+        """(steps done, moves accepted, proposals evaluated); synchronises the device."""
+        a, b, c = c_int64(), c_int64(), c_int64()
+        _native.check(_native.lib().kmc_driver_counters(self._handle, byref(a), byref(b), byref(c)),
+                      "kmc_driver_counters")
+        return a.value, b.value, c.value
 
     def log(self):
         """Selection log, oldest first: (pid [-1 = rejected], target site or charge, dE)."""

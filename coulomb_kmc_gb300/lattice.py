@@ -137,9 +137,23 @@ def _a_coeff(j, k, n, m):
 
 @lru_cache(maxsize=64)
 def dense_operator(L, E):
-    """Dense R (L^2 x L^2), row = l(l+1)+k of the local expansion, col = n(n+1)+m."""
+    """Dense R (L^2 x L^2), row = l(l+1)+k of the local expansion, col = n(n+1)+m.
+
+    The lattice sums are homogeneous in the edge, S_l(E) = S_l(1) E^-(l+1), so R is
+    built once per L for E = 1 and scaled: R(E)[jk, nm] = R(1)[jk, nm] E^-(j+n+1)."""
+    R1 = _unit_operator(int(L))
+    deg = np.array([j for j in range(L) for _ in range(2 * j + 1)], dtype=np.float64)
+    scale = float(E) ** (-(deg[:, None] + deg[None, :] + 1.0))
+    R = R1 * scale
+    R = 0.5 * (R + R.T)
+    R.setflags(write=False)
+    return R
+
+
+@lru_cache(maxsize=8)
+def _unit_operator(L):
     lmax = 2 * L - 1
-    S = lattice_sums(lmax, float(E))
+    S = lattice_sums(lmax, 1.0)
     R = np.zeros((L * L, L * L))
     for j in range(L):
         for k in range(-j, j + 1):

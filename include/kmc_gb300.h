@@ -210,8 +210,9 @@ int kmc_driver_step(kmc_driver *d, int64_t nsteps);
 /* capture one step as a CUDA graph on the system's stream; kmc_driver_launch replays it */
 int kmc_driver_capture(kmc_driver *d);
 int kmc_driver_launch(kmc_driver *d, int64_t nsteps, void *stream);
-/* steps done, moves accepted (synchronises the system's stream) */
-int kmc_driver_counters(kmc_driver *d, int64_t *steps_out, int64_t *accepted_out);
+/* steps done, moves accepted, proposals evaluated (synchronises the system's stream; after
+   kmc_driver_launch on another stream the caller synchronises that stream first; any pointer may be NULL) */
+int kmc_driver_counters(kmc_driver *d, int64_t *steps_out, int64_t *accepted_out, int64_t *proposals_out);
 /* selection log, oldest first: particle id (-1 = rejected), target site (lattice) or -1,
    energy difference of the selected proposal; n_out = entries written */
 int kmc_driver_log(kmc_driver *d, int64_t max_entries, int64_t *pid_out, int64_t *target_out, double *de_out,
@@ -219,6 +220,13 @@ int kmc_driver_log(kmc_driver *d, int64_t max_entries, int64_t *pid_out, int64_t
 /* lattice: site of every charge (host array of n) */
 int kmc_driver_sites(kmc_driver *d, int64_t *sites_out);
 int kmc_driver_free(kmc_driver *d);
+
+/* One round over many systems (serving / batched replicas): replay each
+ * driver's captured step `steps` times, the drivers spread round-robin over
+ * the worker streams, ordered after the work queued on main_stream; main_stream
+ * waits for all of them.  No host synchronisation.  Call from one host thread. */
+int kmc_drivers_launch(kmc_driver **drivers, int64_t n, int64_t steps, void *main_stream, void **worker_streams,
+                       int64_t n_workers);
 
 /* Diagnostic (no reference counterpart): measured FMA throughput of the
  * current device's FP64 (fp64 != 0) or FP32 pipe in TFLOP/s (FMA = 2 flops),
