@@ -53,7 +53,7 @@ class KMCFMM:
         double-FP32 accept contributions added to the FP64 state) or 'mixed_fp64_accept'.
     :arg initial_solve: 'auto' (default), 'exact' (direct particle-to-local sum) or 'fmm'
         (octree P2M/M2M/M2L/L2L, the reference's method, kmc_fmm.py:956-959); 'auto' takes
-        the exact sum while cells x charges x images <= 1e9.
+        the exact sum while cells x charges x images <= 1e8.
     ``shell_width``, ``_debug`` and ``cuda_direct`` are accepted for signature
     compatibility and have no effect (the whole path always runs on the GPU).
     """
@@ -355,4 +355,22 @@ class KMCFMM:
             pass
 
     def eval_field(self, points):
-        raise NotImplementedError("eval_field is not part of this implementation yet")
+        """Potential of all charges at the given (n, 3) points (kmc_fmm.py:544-567); the
+        energy unit is not applied.  numpy in, numpy out; a CUDA tensor in, a CUDA tensor
+        out (no host copy)."""
+        self._assert_init()
+        torch = _torch()
+        self._set_stream()
+        if _is_torch(points) and points.is_cuda:
+            pts = points.detach().to(torch.float64).reshape(-1, 3).contiguous()
+            out = torch.empty(pts.shape[0], dtype=torch.float64, device=pts.device)
+            _native.check(_native.lib().kmc_eval_field(self._handle, pts.shape[0], pts.data_ptr(), out.data_ptr()),
+                          "kmc_eval_field")
+            return out
+        pts = np.atleast_2d(_host(points, np.float64)).reshape(-1, 3)
+        self._check_in_box(pts)
+        d = torch.from_numpy(pts).cuda()
+        out = torch.empty(pts.shape[0], dtype=torch.float64, device="cuda")
+        _native.check(_native.lib().kmc_eval_field(self._handle, pts.shape[0], d.data_ptr(), out.data_ptr()),
+                      "kmc_eval_field")
+        return out.cpu().numpy()

@@ -67,7 +67,7 @@ typedef struct kmc_params {
     int32_t initial_solve;
 } kmc_params;
 
-#define KMC_INIT_AUTO 0  /* exact below 1e9 (cells x charges x images), FMM above */
+#define KMC_INIT_AUTO 0  /* exact up to 1e8 (cells x charges x images), FMM above */
 #define KMC_INIT_EXACT 1 /* direct particle-to-local sum over all charges and images */
 #define KMC_INIT_FMM 2   /* P2M, M2M, M2L, L2L over the octree (FP64) */
 
@@ -169,6 +169,12 @@ int kmc_info(kmc_system *s, int64_t *ncell, int64_t *capacity, int64_t *n);
 int kmc_profile(kmc_system *s, int32_t enable);
 int kmc_profile_read(kmc_system *s, int32_t reset, double *ms_out, int64_t *count_out, int64_t *launches_out);
 const char *kmc_kernel_name(int32_t id);
+
+/* Potential of all charges at n points (device arrays [n][3] and [n]), without
+ * the energy unit: near field of the 27 neighbour cells, the cell's local
+ * expansion and, for pbc, the far-lattice term.  Points must lie in the box.
+ * Replaces KMCFMM.eval_field (kmc_fmm.py:544-567). */
+int kmc_eval_field(kmc_system *s, int64_t n, const double *d_points, double *d_out);
 
 /* Launch-shape tuning (no reference counterpart; the reference has fixed
  * OpenMP loops).  key: KMC_TUNE_*; value 0 restores the built-in choice.

@@ -209,6 +209,12 @@ class OracleKMC:
         self.energy = energy * self.energy_unit
         return self.energy
 
+    def _lr_energy_of(self, M, E):
+        M = np.ascontiguousarray(M, dtype=REAL)
+        E = np.ascontiguousarray(E, dtype=REAL)
+        return lib().orc_lr_energy(c_int64(self.L), _p(self.lr_data), _p(self.lr_indptr), _p(self.lr_indices),
+                                   _p(self.lr_dip), _p(M), _p(E))
+
     def _lr_old_energy(self):
         return lib().orc_lr_energy(c_int64(self.L), _p(self.lr_data), _p(self.lr_indptr), _p(self.lr_indices),
                                    _p(self.lr_dip), _p(self.multipole_exp), _p(self.local_dot_coeffs))
@@ -476,6 +482,35 @@ class OracleKMC:
         self.store, self.store_ids, self.max_occ = st, si, max_occ
 
     # ------------------------------------------------------------------
+    def eval_field(self, points):
+        """KMCFMM.eval_field (kmc_fmm.py:544-567): near field (kmc_local.py:1033-1182),
+        cell local expansion (kmc_octal.py:1417-1440) and, for pbc, the lattice term as
+        the bilinear part of the lattice energy, E(M + m_x) - E(M) - E(m_x)
+        (kmc_full_long_range.py:341-390)."""
+        pts = np.ascontiguousarray(np.atleast_2d(points), dtype=REAL)
+        n = pts.shape[0]
+        ones = np.ones(n, REAL)
+        ids = np.full(n, -1, INT64)
+        cells = np.array([self.lcell(c) for c in self._bin(pts)], dtype=INT64)
+        near = np.zeros(n, REAL)
+        far = np.zeros(n, REAL)
+        self._direct(0, n, pts, ones, ids, cells, near)
+        self._indirect(n, cells, pts, ones, far)
+        out = near + far
+        if self.bc == "pbc":
+            NC = 2 * self.L * self.L
+            e0 = self._lr_old_energy()
+            for i in range(n):
+                mx = np.zeros(NC, REAL)
+                ex = np.zeros(NC, REAL)
+                sph = spherical(tuple(pts[i]))
+                multipole_exp(self.L, sph, 1.0, mx)
+                dot_vec(self.L, sph, 1.0, ex)
+                e_sum = self._lr_energy_of(self.multipole_exp + mx, self.local_dot_coeffs + ex)
+                e_x = self._lr_energy_of(mx, ex)
+                out[i] += e_sum - e0 - e_x
+        return out
+
     def primary_local_expansions(self):
         """Primary-cell expansions in reference layout [ncps^3, 2L^2] (x fastest)."""
         n, p = self.ncps, self.pad
