@@ -180,15 +180,31 @@ __global__ void __launch_bounds__(kSelThreads) k_rate_partial(const long long n,
     if (threadIdx.x == 0) part[blockIdx.x] = red[0];
 }
 
-// inclusive scan of v[0..kPickThreads) in place (Hillis-Steele, fixed order)
+// inclusive scan of v[0..kPickThreads) in place: shuffle scans within warps, then
+// over the warp totals (fixed order, deterministic)
 __device__ void block_scan(double *v)
 {
-    for (int off = 1; off < kPickThreads; off <<= 1) {
-        const double a = ((int)threadIdx.x >= off) ? v[threadIdx.x - off] : 0.0;
-        __syncthreads();
-        v[threadIdx.x] += a;
-        __syncthreads();
+    __shared__ double wsum[kPickThreads / 32];
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    double x = v[t];
+    for (int off = 1; off < 32; off <<= 1) {
+        const double y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
     }
+    if (lane == 31) wsum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        double w = lane < kPickThreads / 32 ? wsum[lane] : 0.0;
+        for (int off = 1; off < 32; off <<= 1) {
+            const double y = __shfl_up_sync(0xffffffffu, w, off);
+            if (lane >= off) w += y;
+        }
+        if (lane < kPickThreads / 32) wsum[lane] = w;
+    }
+    __syncthreads();
+    if (wid > 0) x += wsum[wid - 1];
+    v[t] = x;
+    __syncthreads();
 }
 
 struct SelOut {

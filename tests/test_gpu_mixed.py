@@ -102,3 +102,39 @@ def test_mixed_device_accept_energy_is_fp64():
     assert rel_err(g32.energy, g64.energy) < 1e-12
     g64.free()
     g32.free()
+
+
+@pytest.mark.parametrize("split", [0, 1])
+@pytest.mark.parametrize("groups", [1, 2, 3])
+def test_mixed_kernel_variants(split, groups):
+    """Launch-shape variants (fused or split lattice kernels, source groups of the
+    double-FP32 accept) give the same differences within the mixed tolerance and
+    the same state within 1e-12 after accepts."""
+    from coulomb_kmc_gb300 import _native
+    hs = LatticeHopSystem(side=16, occupancy=0.25, seed=5)
+    (g64, _), (g32, _) = both(hs.positions(), hs.charges(), hs.extent, "pbc", 3, 12, max_move=1.0)
+    lib = _native.lib()
+    assert lib.kmc_set_tuning(g32._handle, 1, split) == 0
+    assert lib.kmc_set_tuning(g32._handle, 0, groups) == 0
+    rng = np.random.default_rng(3)
+    for _ in range(3):
+        ppos, masks, tsite = hs.proposals()
+        smc = np.array([6], np.int64)
+        sites = np.zeros((hs.n, 1), np.int64)
+        d64, d32 = np.zeros((hs.n, 6)), np.zeros((hs.n, 6))
+        g64.propose_with_dats(smc, sites, ppos, masks, d64)
+        g32.propose_with_dats(smc, sites, ppos, masks, d32)
+        act = masks > 0
+        assert rel_err(d32[act], d64[act]).max() < MIXED_TOL
+        pid, h = hs.select(d64, masks, rng, 2.0)
+        mv = ppos[pid, 3 * h:3 * h + 3].copy()
+        g64.accept((pid, mv))
+        g32.accept((pid, mv))
+        hs.occ[hs.site_of[pid]] = -1
+        hs.occ[tsite[pid, h]] = pid
+        hs.site_of[pid] = tsite[pid, h]
+    la, lb = g32.state()["local_expansions"], g64.state()["local_expansions"]
+    assert np.max(np.abs(la - lb)) < 1e-12 * np.max(np.abs(lb))
+    assert rel_err(g32.energy, g64.energy) < 1e-12
+    g64.free()
+    g32.free()
