@@ -156,7 +156,7 @@ __device__ __forceinline__ double rate_of(const long long e, const long long n, 
 
 __global__ void __launch_bounds__(kSelThreads) k_rate_partial(const long long n, const double *__restrict__ diffs,
                                                               const long long *__restrict__ masks, const double hb,
-                                                              double *part, long long *counters)
+                                                              double *part, double *rates, long long *counters)
 {
     __shared__ double red[kSelThreads];
     __shared__ int active;
@@ -166,7 +166,9 @@ __global__ void __launch_bounds__(kSelThreads) k_rate_partial(const long long n,
     double acc = 0.0;
     int na = 0;
     for (int k = 0; k < kSelItems; ++k) {
-        acc += rate_of(base + k, n, diffs, masks, hb);
+        const double r = rate_of(base + k, n, diffs, masks, hb);
+        if (base + k < n) rates[base + k] = r;
+        acc += r;
         na += (base + k < n && masks[base + k]) ? 1 : 0;
     }
     if (na) atomicAdd(&active, na);
@@ -229,7 +231,7 @@ __device__ void log_step(const SelOut &o, const long long st, const long long pi
 
 __global__ void __launch_bounds__(kPickThreads) k_rate_pick(const long long n, const int nb, const int M,
                                                             const double *__restrict__ diffs,
-                                                            const long long *__restrict__ masks, const double hb,
+                                                            const double *__restrict__ rates,
                                                             const double *__restrict__ part,
                                                             const double *__restrict__ ppos, const Key key,
                                                             SelOut o, int *site_of, int *occ,
@@ -289,7 +291,7 @@ __global__ void __launch_bounds__(kPickThreads) k_rate_pick(const long long n, c
     }
     __syncthreads();
     const long long e = (long long)s_blk * kSelChunk + t;
-    const double r = rate_of(e, n, diffs, masks, hb);
+    const double r = e < n ? rates[e] : 0.0;
     __syncthreads();
     sc[t] = r;
     __syncthreads();
@@ -364,7 +366,7 @@ struct kmc_driver {
     int N = 0, M = 1, side = 0, wrap = 0;
     double E = 0.0, spacing = 1.0;
     Key key{};
-    double *ppos = nullptr, *diffs = nullptr, *part = nullptr;
+    double *ppos = nullptr, *diffs = nullptr, *part = nullptr, *rates = nullptr;
     long long *masks = nullptr, *smc = nullptr, *sites = nullptr;
     int *tsite = nullptr, *site_of = nullptr, *occ = nullptr;
     long long *sel_pid = nullptr, *counters = nullptr, *log_pid = nullptr, *log_tgt = nullptr;
@@ -404,8 +406,8 @@ int enqueue_step(kmc_driver *d, cudaStream_t st)
         const long long n = (long long)N * d->M;
         const int nb = (int)((n + kSelChunk - 1) / kSelChunk);
         const double hb = 0.5 * d->prm.beta;
-        k_rate_partial<<<nb, kSelThreads, 0, st>>>(n, d->diffs, d->masks, hb, d->part, d->counters);
-        k_rate_pick<<<1, kPickThreads, 0, st>>>(n, nb, d->M, d->diffs, d->masks, hb, d->part, d->ppos, d->key, o,
+        k_rate_partial<<<nb, kSelThreads, 0, st>>>(n, d->diffs, d->masks, hb, d->part, d->rates, d->counters);
+        k_rate_pick<<<1, kPickThreads, 0, st>>>(n, nb, d->M, d->diffs, d->rates, d->part, d->ppos, d->key, o,
                                                 d->site_of, d->occ, d->tsite);
     } else {
         k_metropolis<<<1, 32, 0, st>>>(N, d->prm.beta, d->diffs, d->ppos, d->key, o);
@@ -502,7 +504,8 @@ int kmc_driver_create(kmc_system *s, const kmc_driver_params *p, kmc_driver **ou
     const size_t nm = (size_t)N * d->M;
     const int nb = (int)((nm + kSelChunk - 1) / kSelChunk);
     const size_t lc = (size_t)p->log_capacity;
-    if (!own(d, &d->ppos, 3 * nm) || !own(d, &d->diffs, nm) || !own(d, &d->masks, nm) || !own(d, &d->smc, 1) ||
+    if (!own(d, &d->ppos, 3 * nm) || !own(d, &d->diffs, nm) || !own(d, &d->rates, nm) || !own(d, &d->masks, nm) ||
+        !own(d, &d->smc, 1) ||
         !own(d, &d->sites, N) || !own(d, &d->part, nb) || !own(d, &d->sel_pid, 1) || !own(d, &d->sel_pos, 3) ||
         !own(d, &d->sel_de, 1) || !own(d, &d->counters, 3) || !own(d, &d->log_pid, lc) || !own(d, &d->log_tgt, lc) ||
         !own(d, &d->log_de, lc)) {

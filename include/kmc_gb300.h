@@ -181,7 +181,8 @@ int kmc_eval_field(kmc_system *s, int64_t n, const double *d_points, double *d_o
  * kmc_autotune times the candidates of every key on scratch buffers of this
  * handle (the handle's state is not changed) and keeps the fastest. */
 #define KMC_TUNE_P2L_GROUPS 0 /* source groups per block of the double-FP32 accept kernel (1..4) */
-#define KMC_TUNE_LR_SPLIT 1   /* mixed pbc lattice term: 0 fused per-charge / per-proposal kernel, 1 two kernels */
+#define KMC_TUNE_LR_FUSED 1   /* mixed pbc lattice term: 0 per-charge and per-proposal kernels, 1 one fused kernel */
+#define KMC_TUNE_LR_STAGE 2   /* fused lattice kernel: 0 folded form in shared memory (when it fits), 1 read-only cache */
 #define KMC_NTUNE 4
 int kmc_set_tuning(kmc_system *s, int32_t key, int32_t value);
 int kmc_get_tuning(kmc_system *s, int32_t key, int32_t *value_out);

@@ -104,9 +104,9 @@ def test_mixed_device_accept_energy_is_fp64():
     g32.free()
 
 
-@pytest.mark.parametrize("split", [0, 1])
+@pytest.mark.parametrize("fused", [0, 1])
 @pytest.mark.parametrize("groups", [1, 2, 3])
-def test_mixed_kernel_variants(split, groups):
+def test_mixed_kernel_variants(fused, groups):
     """Launch-shape variants (fused or split lattice kernels, source groups of the
     double-FP32 accept) give the same differences within the mixed tolerance and
     the same state within 1e-12 after accepts."""
@@ -114,7 +114,7 @@ def test_mixed_kernel_variants(split, groups):
     hs = LatticeHopSystem(side=16, occupancy=0.25, seed=5)
     (g64, _), (g32, _) = both(hs.positions(), hs.charges(), hs.extent, "pbc", 3, 12, max_move=1.0)
     lib = _native.lib()
-    assert lib.kmc_set_tuning(g32._handle, 1, split) == 0
+    assert lib.kmc_set_tuning(g32._handle, 1, fused) == 0
     assert lib.kmc_set_tuning(g32._handle, 0, groups) == 0
     rng = np.random.default_rng(3)
     for _ in range(3):
