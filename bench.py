@@ -142,7 +142,9 @@ def flop_model(kmc, host_sys, lr_nnz_folded):
 # DRAM traffic per launch of the dominant kernel, from the ncu capture summarised in
 # profiles/near_far_cell_fp64_lattice48.md (dram__bytes_read.sum + dram__bytes_write.sum)
 NCU_TRAFFIC = {"near_far_cell": 12.921088e6}
-NCU_TRAFFIC_MIXED = {}
+# mixed path: profiles/k_near_cell_mixed_lattice48.md, k_p2l_df2_lattice48.md, k_lr_mixed_lattice48.md
+NCU_TRAFFIC_MIXED = {"near_far_cell": 13.074688e6, "accept_p2l": 5.233408e6, "far_lattice": 24.304384e6,
+                     "far_lattice_old": 1.036032e6}
 
 
 def kernel_times(kmc):

@@ -142,6 +142,9 @@ class Server:
         self.active = []
         self._cv = threading.Condition()
         self._worker_ptrs = (c_void_p * len(self.workers))(*[s.cuda_stream for s in self.workers])
+        # round timing events, created once (before any system captures its step)
+        self._e0 = torch.cuda.Event(enable_timing=True)
+        self._e1 = torch.cuda.Event(enable_timing=True)
 
     # -- one round over the given slots ------------------------------------
     def round(self, slots):
@@ -150,8 +153,7 @@ class Server:
         if not slots:
             return 0.0
         arr = (c_void_p * len(slots))(*[s.drv._handle.value for s in slots])
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
+        e0, e1 = self._e0, self._e1
         e0.record(self.main)
         _native.check(_native.lib().kmc_drivers_launch(arr, len(slots), 1, c_void_p(self.main.cuda_stream),
                                                        self._worker_ptrs, len(self.workers)),

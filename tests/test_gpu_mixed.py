@@ -48,6 +48,28 @@ def test_mixed_offlattice(bc, L):
     g32.free()
 
 
+@pytest.mark.parametrize("bc", ["free_space", "pbc"])
+def test_mixed_large_box_high_order(bc):
+    """Box edge 64 and L = 16: the FP32 lattice quantities stay in range (box units)."""
+    N, E, M = 600, 64.0, 2
+    rng = np.random.default_rng(8)
+    P = rng.uniform(-0.5 * E, 0.5 * E, (N, 3))
+    Q = neutral_charges(N)
+    (g64, _), (g32, _) = both(P, Q, E, bc, 3, 16, max_move=1.0)
+    smc = np.array([M], np.int64)
+    sites = np.zeros((N, 1), np.int64)
+    masks = np.ones((N, M), np.int64)
+    ppos = np.clip(np.repeat(P, M, axis=0).reshape(N, 3 * M) + rng.uniform(-1.0, 1.0, (N, 3 * M)),
+                   -0.5 * E, 0.5 * E)
+    d64, d32 = np.zeros((N, M)), np.zeros((N, M))
+    g64.propose_with_dats(smc, sites, ppos, masks, d64)
+    g32.propose_with_dats(smc, sites, ppos, masks, d32)
+    assert np.all(np.isfinite(d32))
+    assert rel_err(d32, d64).max() < MIXED_TOL
+    g64.free()
+    g32.free()
+
+
 @pytest.mark.parametrize("mode", ["mixed", "mixed_fp64_accept"])
 def test_mixed_lattice_and_accepts(mode):
     """pbc lattice hops: mixed differences within 1e-6; after accepting the same
