@@ -140,7 +140,7 @@ def flop_model(kmc, host_sys, lr_nnz_folded):
 
 
 # DRAM traffic per launch of the dominant kernel, from the ncu capture summarised in
-# profiles/near_far_cell_fp64_lattice48.md (dram__bytes_read.sum + dram__bytes_write.sum)
+# profiles/fp64_step_lattice48_launch_list.md (dram__bytes_read.sum + dram__bytes_write.sum)
 NCU_TRAFFIC = {"near_far_cell": 12.921088e6}
 # mixed path: profiles/k_near_cell_mixed_lattice48.md, k_p2l_df2_lattice48.md, k_lr_mixed_lattice48.md
 NCU_TRAFFIC_MIXED = {"near_far_cell": 13.074688e6, "accept_p2l": 5.233408e6, "far_lattice": 24.304384e6,
@@ -446,12 +446,14 @@ def bench_serving(args):
         print(json.dumps({"rate": rate, **st}), file=sys.stderr)
     reqs = poisson_requests(args.requests, args.rates[0], seed=4, n_range=(1000, args.max_n),
                             k_range=(10, args.max_k))
-    p64, s64 = one_at_a_time(reqs, "fp64")
+    p64, s64, w64 = one_at_a_time(reqs, "fp64")
     base = p64 / s64
     line = {"metric": METRIC, "workload": "serving", "unit": UNIT,
             "value": max(v["proposals_per_s"] for v in out.values()),
             "fp64_one_at_a_time": base,
+            "fp64_one_at_a_time_with_builds": p64 / w64,
             "mixed_vs_fp64": max(v["proposals_per_s"] for v in out.values()) / base,
+            "mixed_vs_fp64_with_builds": max(v["proposals_per_s"] for v in out.values()) / (p64 / w64),
             "per_rate": out,
             "config": {"workload": f"{args.requests} requests (seed 4), Poisson arrivals, N log-uniform in "
                                    f"[1000, {args.max_n}], lattice-hop pbc or off-lattice free_space with "
@@ -480,10 +482,10 @@ def main():
     ap.add_argument("--systems", type=int, default=64)
     ap.add_argument("--rounds", type=int, default=20)
     ap.add_argument("--workers", type=int, default=8)
-    ap.add_argument("--requests", type=int, default=48)
+    ap.add_argument("--requests", type=int, default=16)
     ap.add_argument("--rates", type=float, nargs="+", default=[50.0, 2000.0])
     ap.add_argument("--max-n", type=int, default=262144)
-    ap.add_argument("--max-k", type=int, default=100)
+    ap.add_argument("--max-k", type=int, default=1000)
     ap.add_argument("--max-active", type=int, default=64)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)

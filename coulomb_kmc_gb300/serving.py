@@ -3,9 +3,9 @@
 A request asks for K propose/accept rounds of one KMC system (lattice hopping
 or off-lattice moves).  The server
 
-* admits requests as slots and HBM budget free up: an admission thread builds
-  the system (charges, initial solve, device driver, captured step graph) on
-  its own CUDA stream while the GPU keeps running the live systems' rounds;
+* admits requests as slots and HBM budget free up: admission threads build
+  systems (charges, initial solve, device driver, captured step graph), each
+  on its own CUDA stream, while the GPU keeps running the live systems' rounds;
 * runs rounds: every live system advances one KMC step per round, all of them
   in one host call (``kmc_drivers_launch``: each system's captured step graph
   on one of a pool of worker streams, so small systems overlap on the device);
@@ -127,7 +127,8 @@ class _null:
 
 
 class Server:
-    def __init__(self, precision="mixed", hbm_budget=150e9, max_active=64, n_workers=8, keep_results=False):
+    def __init__(self, precision="mixed", hbm_budget=150e9, max_active=64, n_workers=8, keep_results=False,
+                 n_admit=4):
         import torch
         self.precision = precision
         self.keep_results = bool(keep_results)
@@ -137,8 +138,11 @@ class Server:
         self.max_active = int(max_active)
         self.workers = [torch.cuda.Stream() for _ in range(int(n_workers))]
         self.main = torch.cuda.Stream()
-        self.admit_stream = torch.cuda.Stream()
+        # admission threads, each building systems on its own stream
+        self.admit_streams = [torch.cuda.Stream() for _ in range(max(1, int(n_admit)))]
+        self.build_s = []
         self.used = 0.0
+        self.reserved = 0  # slots taken by systems being built, waiting or running
         self.active = []
         self._cv = threading.Condition()
         self._worker_ptrs = (c_void_p * len(self.workers))(*[s.cuda_stream for s in self.workers])
@@ -164,8 +168,10 @@ class Server:
             s.done += 1
         return e0.elapsed_time(e1)
 
-    def admit(self, req):
-        k, d = build_system(req, self.precision, self.admit_stream)
+    def admit(self, req, stream=None):
+        t0 = time.perf_counter()
+        k, d = build_system(req, self.precision, stream if stream is not None else self.admit_streams[0])
+        self.build_s.append(time.perf_counter() - t0)
         nb = estimate_bytes(k.N, req.kind, req.L, k.R)
         return Slot(req=req, kmc=k, drv=d, nbytes=nb, admitted=time.perf_counter())
 
@@ -209,7 +215,7 @@ class Server:
                     self.used -= s.nbytes
                     self._cv.notify_all()
 
-        def admission():
+        def admission(stream):
             torch.cuda.set_device(torch.cuda.current_device())
             while not stop.is_set():
                 bury()
@@ -222,8 +228,7 @@ class Server:
                     errors.append(MemoryError("request %d needs %.3g bytes, above the budget" % (r.rid, need)))
                     continue
                 with self._cv:
-                    while not stop.is_set() and (self.used + need > self.budget or
-                                                 len(self.active) + ready.qsize() >= self.max_active):
+                    while not stop.is_set() and (self.used + need > self.budget or self.reserved >= self.max_active):
                         self._cv.wait(timeout=0.01)
                         self._cv.release()
                         try:
@@ -231,18 +236,21 @@ class Server:
                         finally:
                             self._cv.acquire()
                     self.used += need
+                    self.reserved += 1
                 try:
-                    s = self.admit(r)
+                    s = self.admit(r, stream)
                     s.nbytes = need
                     ready.put(s)
                 except Exception as e:  # surfaced in the main loop
                     errors.append(e)
                     with self._cv:
                         self.used -= need
+                        self.reserved -= 1
 
-        th = threading.Thread(target=admission, daemon=True)
+        threads = [threading.Thread(target=admission, args=(st,), daemon=True) for st in self.admit_streams]
         t0 = time.perf_counter()
-        th.start()
+        for th in threads:
+            th.start()
         pending = list(reqs)
         round_ms, round_wall, finished = [], [], []
         proposals = 0.0
@@ -275,6 +283,8 @@ class Server:
                 if done:
                     with self._cv:
                         self.active = [s for s in self.active if s.done < s.req.rounds]
+                        self.reserved -= len(done)
+                        self._cv.notify_all()
                     for s in done:
                         st = self.retire(s, free=False)
                         proposals += st[2]
@@ -283,7 +293,8 @@ class Server:
                         graveyard.put(s)
         finally:
             stop.set()
-            th.join(timeout=60)
+            for th in threads:
+                th.join(timeout=60)
             bury()
         wall = time.perf_counter() - (busy_t0 if busy_t0 else t0)
         lat = np.array([s.finished - s.req.arrival for s in finished])
@@ -296,14 +307,19 @@ class Server:
             "round_wall_ms_p99": float(np.percentile(round_wall, 99)) if round_wall else 0.0,
             "request_latency_s_p50": float(np.percentile(lat, 50)) if len(lat) else 0.0,
             "request_latency_s_p99": float(np.percentile(lat, 99)) if len(lat) else 0.0,
+            "build_s_p50": float(np.percentile(self.build_s, 50)) if self.build_s else 0.0,
+            "build_s_p99": float(np.percentile(self.build_s, 99)) if self.build_s else 0.0,
+            "admission_threads": len(self.admit_streams),
         }
 
 
 def one_at_a_time(requests, precision="fp64"):
     """Baseline: each request alone, in arrival order, its K steps as one
-    captured-graph replay; returns (proposals, device seconds of the steps)."""
+    captured-graph replay; returns (proposals, device seconds of the steps,
+    wall seconds including each system's build)."""
     import torch
     total_p, total_s = 0.0, 0.0
+    w0 = time.perf_counter()
     for r in sorted(requests, key=lambda r: r.arrival):
         k, d = build_system(r, precision)
         e0 = torch.cuda.Event(enable_timing=True)
@@ -317,7 +333,7 @@ def one_at_a_time(requests, precision="fp64"):
         total_p += d.stats()[2]
         d.free()
         k.free()
-    return total_p, total_s
+    return total_p, total_s, time.perf_counter() - w0
 
 
 def poisson_requests(count, rate, seed, n_range=(1000, 262144), k_range=(10, 1000), L=12):
