@@ -91,6 +91,10 @@ SIGNATURES = {
     "kmc_profile_read": ([c_void_p, c_int32, c_void_p, c_void_p, POINTER(c_int64)], c_int),
     "kmc_kernel_name": ([c_int32], c_char_p),
     "kmc_eval_field": ([c_void_p, c_int64, c_void_p, c_void_p], c_int),
+    "kmc_get_energy_ids": ([c_void_p, c_int64, c_void_p, c_void_p], c_int),
+    "kmc_group_energy": ([c_void_p, c_int64, c_void_p, c_void_p, c_void_p], c_int),
+    "kmc_extract": ([c_void_p, c_int64, c_void_p, POINTER(c_double)], c_int),
+    "kmc_inject": ([c_void_p, c_int64, c_void_p, c_void_p, POINTER(c_double)], c_int),
     "kmc_set_tuning": ([c_void_p, c_int32, c_int32], c_int),
     "kmc_get_tuning": ([c_void_p, c_int32, POINTER(c_int32)], c_int),
     "kmc_driver_create": ([c_void_p, POINTER(KmcDriverParams), POINTER(c_void_p)], c_int),

@@ -354,6 +354,137 @@ class KMCFMM:
         except Exception:
             pass
 
+    # ------------------------------------------------------------------
+    # insertion and removal of charges (InjectorExtractor, kmc_inject_extract.py)
+    def get_energy(self, ids):
+        """Energy of groups of charges in the system: ``ids`` (n, m) local ids, returns the
+        n sums of q_i phi_i (phi without the charge itself) times the energy unit
+        (kmc_inject_extract.py:82-123)."""
+        self._assert_init()
+        torch = _torch()
+        ids = np.atleast_2d(np.asarray(ids, dtype=np.int64))
+        flat = np.ascontiguousarray(ids.ravel())
+        if flat.size == 0:
+            return np.zeros(ids.shape[0])
+        if np.any(flat < 0) or np.any(flat >= self.N):
+            raise IndexError("charge id out of range")
+        self._set_stream()
+        d_ids = torch.from_numpy(flat).cuda()
+        out = torch.empty(flat.size, dtype=torch.float64, device="cuda")
+        _native.check(_native.lib().kmc_get_energy_ids(self._handle, flat.size, d_ids.data_ptr(), out.data_ptr()),
+                      "kmc_get_energy_ids")
+        return out.cpu().numpy().reshape(ids.shape).sum(axis=1)
+
+    def get_energy_with_dats(self, masks, energy):
+        """Write get_energy of every charge with a positive mask into ``energy``
+        (kmc_inject_extract.py:125-142)."""
+        m = _host(array_of(masks), np.int64).reshape(self.N, -1)[:, 0]
+        ids = np.nonzero(m > 0)[0]
+        e = self.get_energy(ids.reshape(-1, 1))
+        tgt = array_of(energy)
+        if _is_torch(tgt):
+            tgt[ids, 0] = _torch().from_numpy(e).to(tgt.device, tgt.dtype)
+        else:
+            tgt[ids, 0] = e
+
+    def compute_energy(self, positions, charges):
+        """Energy of a small set of charges alone in the box (the reference's direct
+        solvers, kmc_inject_extract.py:145-166), times the energy unit."""
+        torch = _torch()
+        pos = np.ascontiguousarray(np.atleast_2d(_host(positions, np.float64)).reshape(-1, 3))
+        q = np.ascontiguousarray(_host(charges, np.float64).reshape(-1))
+        if q.shape[0] != pos.shape[0]:
+            raise ValueError("positions and charges differ in length")
+        self._set_stream()
+        dp, dq = torch.from_numpy(pos).cuda(), torch.from_numpy(q).cuda()
+        out = torch.zeros(1, dtype=torch.float64, device="cuda")
+        _native.check(_native.lib().kmc_group_energy(self._handle, q.shape[0], dp.data_ptr(), dq.data_ptr(),
+                                                      out.data_ptr()), "kmc_group_energy")
+        return float(out.item())
+
+    def propose_extract(self, ids, self_energy=True):
+        """Energy change of removing each group of charges (rows of ``ids``)
+        (kmc_inject_extract.py:178-214)."""
+        self._assert_init()
+        ids = np.atleast_2d(np.asarray(ids, dtype=np.int64))
+        if ids.size == 0:
+            return np.array(())
+        group = self.get_energy(ids)
+        pos = self._positions_now()
+        q = self._charges_now()
+        out = np.zeros(ids.shape[0])
+        for g in range(ids.shape[0]):
+            bb = self.compute_energy(pos[ids[g]], q[ids[g]]) if self_energy else 0.0
+            out[g] = bb - group[g]
+        return out
+
+    def propose_inject(self, positions, charges):
+        """Energy change of adding the charges (kmc_inject_extract.py:217-237)."""
+        self._assert_init()
+        pos = np.atleast_2d(_host(positions, np.float64)).reshape(-1, 3)
+        q = _host(charges, np.float64).reshape(-1)
+        bb = self.compute_energy(pos, q)
+        phi = self.eval_field(pos)
+        return bb + self.energy_unit * float(np.sum(q * phi))
+
+    def extract(self, ids=()):
+        """Remove the charges ``ids`` (kmc_inject_extract.py:240-301); the others keep
+        their order and the positions / charges dats are shortened accordingly."""
+        self._assert_init()
+        ids = np.ascontiguousarray(np.asarray(ids, dtype=np.int64).ravel())
+        if ids.size == 0:
+            return
+        self._set_stream()
+        de = c_double()
+        _native.check(_native.lib().kmc_extract(self._handle, ids.size, ids.ctypes.data, byref(de)), "kmc_extract")
+        keep = np.setdiff1d(np.arange(self.N), ids)
+        self._replace_rows(keep, None, None)
+        self._energy_valid = False
+
+    def inject(self, add):
+        """Add charges, appended after the existing ones (kmc_inject_extract.py:304-424).
+        ``add`` maps the positions and charges dats to the new rows (as the reference's
+        ``state.modifier.add``) or is a (positions, charges) pair."""
+        self._assert_init()
+        if isinstance(add, dict):
+            pos, q = add[self.positions], add[self.charges]
+        else:
+            pos, q = add
+        pos = np.ascontiguousarray(np.atleast_2d(_host(pos, np.float64)).reshape(-1, 3))
+        q = np.ascontiguousarray(_host(q, np.float64).reshape(-1))
+        if q.shape[0] != pos.shape[0] or q.shape[0] == 0:
+            raise ValueError("inject needs as many charges as positions")
+        self._check_in_box(pos)
+        self._set_stream()
+        de = c_double()
+        _native.check(_native.lib().kmc_inject(self._handle, q.shape[0], pos.ctypes.data, q.ctypes.data, byref(de)),
+                      "kmc_inject")
+        self._replace_rows(np.arange(self.N), pos, q)
+        self._energy_valid = False
+
+    def _positions_now(self):
+        return self.state()["positions"]
+
+    def _charges_now(self):
+        return _host(array_of(self.charges), np.float64).reshape(self.N, -1)[:, 0]
+
+    def _replace_rows(self, keep, add_pos, add_q):
+        """Host dats after extract (rows ``keep``) or inject (rows appended)."""
+        pos = self.state()["positions"]
+        q = self._charges_now()[keep]
+        if add_q is not None:
+            q = np.concatenate([q, add_q])
+        self.N = pos.shape[0]
+        for attr, new in (("positions", pos), ("charges", q.reshape(-1, 1))):
+            obj = getattr(self, attr)
+            if hasattr(obj, "data") and isinstance(getattr(obj, "data"), np.ndarray):
+                obj.data = new.copy()
+            elif _is_torch(obj):
+                setattr(self, attr, _torch().from_numpy(new.copy()).to(obj.device))
+            else:
+                setattr(self, attr, new.copy())
+        self._charges_host = q.copy()
+
     def eval_field(self, points):
         """Potential of all charges at the given (n, 3) points (kmc_fmm.py:544-567); the
         energy unit is not applied.  numpy in, numpy out; a CUDA tensor in, a CUDA tensor

@@ -176,6 +176,31 @@ const char *kmc_kernel_name(int32_t id);
  * Replaces KMCFMM.eval_field (kmc_fmm.py:544-567). */
 int kmc_eval_field(kmc_system *s, int64_t n, const double *d_points, double *d_out);
 
+/* ------------------------------------------------------------------------
+ * Insertion and removal of charges (InjectorExtractor, kmc_inject_extract.py).
+ * ------------------------------------------------------------------------ */
+/* Energy of each listed charge in the system, q_i times its potential without
+ * itself (near field, cell expansion, lattice term), times the energy unit.
+ * Device arrays.  Replaces InjectorExtractor.get_energy (kmc_inject_extract.py:82-123). */
+int kmc_get_energy_ids(kmc_system *s, int64_t n, const int64_t *d_ids, double *d_out);
+/* Energy of n charges alone in the box under the system's boundary condition and
+ * energy definition (pair terms over the 3x3x3 image block for '27'/pbc with the
+ * self-image terms, and the lattice term for pbc), times the energy unit; device
+ * arrays, result in d_out[0].  Replaces compute_energy (kmc_inject_extract.py:145-166,
+ * ppmd FreeSpaceDirect / NearestDirect / PBCDirect). */
+int kmc_group_energy(kmc_system *s, int64_t n, const double *d_positions, const double *d_charges, double *d_out);
+/* Remove the listed charges (host ids): the energy changes by their set energy
+ * minus their energies in the system; the expansions lose their contributions;
+ * the remaining charges keep their order (higher ids shift down).  Synchronous.
+ * Replaces InjectorExtractor.extract (kmc_inject_extract.py:240-301). */
+int kmc_extract(kmc_system *s, int64_t n, const int64_t *ids, double *de_out);
+/* Add n charges (host arrays), appended with ids N..N+n-1: the energy changes by
+ * their set energy plus their charges times the field at their positions.
+ * Synchronous.  Replaces InjectorExtractor.inject (kmc_inject_extract.py:304-424).
+ * Both calls reallocate the system's charge arrays: a captured driver graph of the
+ * system must be recreated afterwards. */
+int kmc_inject(kmc_system *s, int64_t n, const double *positions, const double *charges, double *de_out);
+
 /* Launch-shape tuning (no reference counterpart; the reference has fixed
  * OpenMP loops).  key: KMC_TUNE_*; value 0 restores the built-in choice.
  * kmc_autotune times the candidates of every key on scratch buffers of this

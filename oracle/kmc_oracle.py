@@ -498,18 +498,82 @@ class OracleKMC:
         self._indirect(n, cells, pts, ones, far)
         out = near + far
         if self.bc == "pbc":
-            NC = 2 * self.L * self.L
-            e0 = self._lr_old_energy()
-            for i in range(n):
-                mx = np.zeros(NC, REAL)
-                ex = np.zeros(NC, REAL)
-                sph = spherical(tuple(pts[i]))
-                multipole_exp(self.L, sph, 1.0, mx)
-                dot_vec(self.L, sph, 1.0, ex)
-                e_sum = self._lr_energy_of(self.multipole_exp + mx, self.local_dot_coeffs + ex)
-                e_x = self._lr_energy_of(mx, ex)
-                out[i] += e_sum - e0 - e_x
+            out += self._lr_potential(pts)
         return out
+
+    def _lr_potential(self, pts):
+        """Lattice part of the potential: bilinear part of the lattice energy for a unit charge."""
+        NC = 2 * self.L * self.L
+        e0 = self._lr_old_energy()
+        out = np.zeros(len(pts))
+        for i in range(len(pts)):
+            mx = np.zeros(NC, REAL)
+            ex = np.zeros(NC, REAL)
+            sph = spherical(tuple(pts[i]))
+            multipole_exp(self.L, sph, 1.0, mx)
+            dot_vec(self.L, sph, 1.0, ex)
+            out[i] = (self._lr_energy_of(self.multipole_exp + mx, self.local_dot_coeffs + ex) - e0 -
+                      self._lr_energy_of(mx, ex))
+        return out
+
+    def get_energy(self, ids):
+        """InjectorExtractor.get_energy (kmc_inject_extract.py:82-123): per group the sum
+        of U0D + U0I + U0L of its charges (kmcl / kmco / lr get_old_energy)."""
+        ids = np.atleast_2d(np.asarray(ids, dtype=INT64))
+        flat = ids.ravel()
+        n = flat.size
+        pos = np.ascontiguousarray(self.positions[flat], dtype=REAL)
+        q = np.ascontiguousarray(self.charges[flat], dtype=REAL)
+        gid = np.ascontiguousarray(self.ids[flat], dtype=INT64)
+        cells = np.array([self.lcell(self.fmm_cells[i]) for i in flat], dtype=INT64)
+        d = np.zeros(n, REAL)
+        f = np.zeros(n, REAL)
+        self._direct(1, n, pos, q, gid, cells, d)
+        self._indirect(n, cells, pos, q, f)
+        e = d + f
+        if self.bc == "pbc":
+            e += q * self._lr_potential(pos)
+        return (e * self.energy_unit).reshape(ids.shape).sum(axis=1)
+
+    def compute_energy(self, positions, charges):
+        """Energy of a set of charges alone in the box: pairs (3x3x3 image block for '27'
+        and pbc, with self images), plus for pbc the lattice energy of the set's
+        multipole (this oracle's definition of the reference's direct solvers)."""
+        P = np.atleast_2d(np.asarray(positions, dtype=REAL))
+        Q = np.asarray(charges, dtype=REAL).ravel()
+        e = 0.0
+        n = len(Q)
+        shifts = [np.zeros(3)] if self.bc == "free_space" else [
+            np.array([a, b, c]) * self.extent for c in (-1, 0, 1) for b in (-1, 0, 1) for a in (-1, 0, 1)]
+        for i in range(n):
+            for j in range(n):
+                for sft in shifts:
+                    if i == j and not np.any(sft):
+                        continue
+                    e += 0.5 * Q[i] * Q[j] / np.linalg.norm(P[i] - P[j] + sft)
+        if self.bc == "pbc":
+            NC = 2 * self.L * self.L
+            M = np.zeros(NC, REAL)
+            Ev = np.zeros(NC, REAL)
+            for i in range(n):
+                sph = spherical(tuple(P[i]))
+                multipole_exp(self.L, sph, Q[i], M)
+                dot_vec(self.L, sph, Q[i], Ev)
+            e += self._lr_energy_of(M, Ev)
+        return e * self.energy_unit
+
+    def propose_extract(self, ids, self_energy=True):
+        """InjectorExtractor.propose_extract (kmc_inject_extract.py:178-214)."""
+        ids = np.atleast_2d(np.asarray(ids, dtype=INT64))
+        g = self.get_energy(ids)
+        return np.array([(self.compute_energy(self.positions[r], self.charges[r]) if self_energy else 0.0) - g[k]
+                         for k, r in enumerate(ids)])
+
+    def propose_inject(self, positions, charges):
+        """InjectorExtractor.propose_inject (kmc_inject_extract.py:217-237)."""
+        P = np.atleast_2d(np.asarray(positions, dtype=REAL))
+        Q = np.asarray(charges, dtype=REAL).ravel()
+        return self.compute_energy(P, Q) + self.energy_unit * float(np.sum(Q * self.eval_field(P)))
 
     def primary_local_expansions(self):
         """Primary-cell expansions in reference layout [ncps^3, 2L^2] (x fastest)."""
