@@ -145,6 +145,24 @@ NCU_TRAFFIC = {"near_far_cell": 12.921088e6}
 # mixed path: profiles/k_near_cell_mixed_lattice48.md, k_p2l_df2_lattice48.md, k_lr_mixed_lattice48.md
 NCU_TRAFFIC_MIXED = {"near_far_cell": 13.074688e6, "accept_p2l": 5.233408e6, "far_lattice": 24.304384e6,
                      "far_lattice_old": 1.036032e6}
+# warp instructions per launch from the same ncu capture (smsp__inst_executed.sum), for the
+# issue-slot fraction of the mixed kernels (4 warp instructions per SM per clock)
+NCU_INST_MIXED = {"near_far_cell": 115.812643e6, "accept_p2l": 78.166604e6, "far_lattice": 26.509679e6,
+                  "far_lattice_old": 17.393185e6}
+
+
+def issue_fracs(per_launch_ms, clk):
+    """Issue-slot fraction of the mixed kernels: ncu warp instructions per launch over
+    the live launch time, against 4 warp instructions per SM per clock at the
+    sampled SM clock."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = (clk or {}).get("sm_mhz") or 2070.0
+    out = {}
+    for k, inst in NCU_INST_MIXED.items():
+        if k in per_launch_ms:
+            out[k] = round(inst / (per_launch_ms[k] * 1e-3) / (sms * 4 * mhz * 1e6), 4)
+    return out
 
 
 def kernel_times(kmc):
@@ -569,6 +587,7 @@ def main():
             "flops_per_launch": fm.get(top),
             "per_kernel_ms": {k: round(v, 5) for k, v in per_launch.items()},
             "per_kernel_tflops": {k: round(v, 4) for k, v in ach.items()},
+            "issue_frac": issue_fracs(per_launch, clk) if args.precision == "mixed" else None,
             "mean_neighbours_per_proposal": fm["mean_neighbours"]}
         drv.free()
         kmc.free()
