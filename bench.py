@@ -266,7 +266,7 @@ def make_system(side, rank, precision, local):
     return hs, kmc, drv, init_s
 
 
-DRIVER_KERNELS_PER_STEP = 3  # proposal generation, rate partial sums, pick
+DRIVER_KERNELS_PER_STEP = 2  # proposal generation, rate sums + pick (one launch)
 
 
 def timed_loop(kmc, drv, steps, warmup, flush, sampler=None, graph=True):

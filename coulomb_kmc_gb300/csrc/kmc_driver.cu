@@ -25,10 +25,11 @@
 namespace {
 
 constexpr int kGenThreads = 128;
-constexpr int kSelThreads = 256;                      // rate partial sums: threads per block
-constexpr int kSelItems = 4;                          // entries per thread
-constexpr int kSelChunk = kSelThreads * kSelItems;    // entries per partial sum
-constexpr int kPickThreads = kSelChunk;               // one entry per thread in the final pick
+// Entries per partial sum, one per thread of a selection block.  256 spreads the
+// FP64 exp (about 19 SM cycles per warp instruction on this part) evenly: a
+// 165,888-entry step makes 648 blocks, 4.3 per SM.
+constexpr int kSelChunk = 256;
+constexpr int kPickThreads = kSelChunk;
 constexpr int kMaxAttempts = 32;                      // re-draws of an off-lattice move that left the box
 
 enum { TAG_DISP_XY = 1, TAG_DISP_Z = 2, TAG_SELECT = 3 };
@@ -78,35 +79,35 @@ __device__ __forceinline__ P4 draw(const Key k, const long long step, const uint
 // ---------------------------------------------------------------------------
 // hop order +x, -x, +y, -y, +z, -z (examples/propose_with_dats_example.py:265-290);
 // periodic systems wrap, a free-space lattice masks hops that leave it
+// one thread per (charge, hop): the six nearest-neighbour sites of each charge,
+// the hop's mask (target inside the box, vacant) and the target's centre
 __global__ void k_lat_gen(const int N, const int side, const double spacing, const double half_e, const int wrap,
                           const int *__restrict__ site_of, const int *__restrict__ occ, double *ppos,
                           long long *masks, int *tsite)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= 6 * N) return;
+    const int i = g / 6, h = g - 6 * i;
     const int s = site_of[i];
-    const int x = s % side, y = (s / side) % side, z = s / (side * side);
-    for (int h = 0; h < 6; ++h) {
-        int t[3] = {x, y, z};
-        const int ax = h >> 1, dir = (h & 1) ? -1 : 1;
-        t[ax] += dir;
-        bool ok = true;
-        if (t[ax] < 0 || t[ax] >= side) {
-            if (wrap)
-                t[ax] = (t[ax] + side) % side;
-            else
-                ok = false;
-        }
-        const int ts = ok ? t[0] + side * (t[1] + side * t[2]) : s;
-        tsite[6 * (size_t)i + h] = ts;
-        masks[6 * (size_t)i + h] = (ok && occ[ts] < 0) ? 1 : 0;
-        const int tx = ts % side, ty = (ts / side) % side, tz = ts / (side * side);
-        double *o = ppos + 18 * (size_t)i + 3 * h;
-        // explicit roundings (no contraction) so that host code reproduces the positions bit for bit
-        o[0] = __dadd_rn(__dsub_rn(__dmul_rn((double)tx, spacing), half_e), __dmul_rn(0.5, spacing));
-        o[1] = __dadd_rn(__dsub_rn(__dmul_rn((double)ty, spacing), half_e), __dmul_rn(0.5, spacing));
-        o[2] = __dadd_rn(__dsub_rn(__dmul_rn((double)tz, spacing), half_e), __dmul_rn(0.5, spacing));
+    int t[3] = {s % side, (s / side) % side, s / (side * side)};
+    const int ax = h >> 1, dir = (h & 1) ? -1 : 1;
+    t[ax] += dir;
+    bool ok = true;
+    if (t[ax] < 0 || t[ax] >= side) {
+        if (wrap)
+            t[ax] = (t[ax] + side) % side;
+        else
+            ok = false;
     }
+    const int ts = ok ? t[0] + side * (t[1] + side * t[2]) : s;
+    tsite[g] = ts;
+    masks[g] = (ok && occ[ts] < 0) ? 1 : 0;
+    const int tx = ts % side, ty = (ts / side) % side, tz = ts / (side * side);
+    double *o = ppos + 3 * (size_t)g;
+    // explicit roundings (no contraction) so that host code reproduces the positions bit for bit
+    o[0] = __dadd_rn(__dsub_rn(__dmul_rn((double)tx, spacing), half_e), __dmul_rn(0.5, spacing));
+    o[1] = __dadd_rn(__dsub_rn(__dmul_rn((double)ty, spacing), half_e), __dmul_rn(0.5, spacing));
+    o[2] = __dadd_rn(__dsub_rn(__dmul_rn((double)tz, spacing), half_e), __dmul_rn(0.5, spacing));
 }
 
 // one displacement uniform in [-step, step]^3 per charge, re-drawn while it
@@ -152,34 +153,6 @@ __device__ __forceinline__ double rate_of(const long long e, const long long n, 
                                           const long long *masks, const double hb)
 {
     return (e < n && masks[e]) ? exp(-hb * diffs[e]) : 0.0;
-}
-
-__global__ void __launch_bounds__(kSelThreads) k_rate_partial(const long long n, const double *__restrict__ diffs,
-                                                              const long long *__restrict__ masks, const double hb,
-                                                              double *part, double *rates, long long *counters)
-{
-    __shared__ double red[kSelThreads];
-    __shared__ int active;
-    if (threadIdx.x == 0) active = 0;
-    __syncthreads();
-    const long long base = (long long)blockIdx.x * kSelChunk + (long long)threadIdx.x * kSelItems;
-    double acc = 0.0;
-    int na = 0;
-    for (int k = 0; k < kSelItems; ++k) {
-        const double r = rate_of(base + k, n, diffs, masks, hb);
-        if (base + k < n) rates[base + k] = r;
-        acc += r;
-        na += (base + k < n && masks[base + k]) ? 1 : 0;
-    }
-    if (na) atomicAdd(&active, na);
-    red[threadIdx.x] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) atomicAdd((unsigned long long *)&counters[2], (unsigned long long)active);
-    for (int w = kSelThreads / 2; w > 0; w >>= 1) {
-        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
 }
 
 // inclusive scan of v[0..kPickThreads) in place: shuffle scans within warps, then
@@ -229,13 +202,12 @@ __device__ void log_step(const SelOut &o, const long long st, const long long pi
     }
 }
 
-__global__ void __launch_bounds__(kPickThreads) k_rate_pick(const long long n, const int nb, const int M,
-                                                            const double *__restrict__ diffs,
-                                                            const double *__restrict__ rates,
-                                                            const double *__restrict__ part,
-                                                            const double *__restrict__ ppos, const Key key,
-                                                            SelOut o, int *site_of, int *occ,
-                                                            const int *__restrict__ tsite)
+// The pick, run by the last selection block to finish: the partial sums and the
+// rates of the other blocks are read through L2 (__ldcg), after their writers'
+// __threadfence.
+__device__ void rate_pick(const long long n, const int nb, const int M, const double *__restrict__ diffs,
+                          const double *rates, const double *part, const double *__restrict__ ppos, const Key key,
+                          const SelOut &o, int *site_of, int *occ, const int *__restrict__ tsite)
 {
     __shared__ double sc[kPickThreads];
     __shared__ double s_target, s_base;
@@ -246,7 +218,7 @@ __global__ void __launch_bounds__(kPickThreads) k_rate_pick(const long long n, c
     const int per = (nb + kPickThreads - 1) / kPickThreads;
     const int b0 = min(nb, t * per), b1 = min(nb, b0 + per);
     double run = 0.0;
-    for (int b = b0; b < b1; ++b) run += part[b];
+    for (int b = b0; b < b1; ++b) run += __ldcg(part + b);
     sc[t] = run;
     if (t == 0) {
         s_blk = -1;
@@ -267,12 +239,13 @@ __global__ void __launch_bounds__(kPickThreads) k_rate_pick(const long long n, c
         if (b1 > b0 && excl <= target && target < sc[t]) {
             double acc = excl;
             for (int b = b0; b < b1; ++b) {
-                if (acc + part[b] > target && part[b] > 0.0) {
+                const double pb = __ldcg(part + b);
+                if (acc + pb > target && pb > 0.0) {
                     s_blk = b;
                     s_base = acc;
                     break;
                 }
-                acc += part[b];
+                acc += pb;
             }
         }
     }
@@ -281,17 +254,18 @@ __global__ void __launch_bounds__(kPickThreads) k_rate_pick(const long long n, c
         // target at or beyond the rounded total: the last block with a non-zero rate
         double acc = 0.0;
         for (int b = 0; b < nb; ++b) {
-            if (part[b] > 0.0) {
+            const double pb = __ldcg(part + b);
+            if (pb > 0.0) {
                 s_blk = b;
                 s_base = acc;
             }
-            acc += part[b];
+            acc += pb;
         }
         if (s_blk < 0) s_blk = 0;
     }
     __syncthreads();
     const long long e = (long long)s_blk * kSelChunk + t;
-    const double r = e < n ? rates[e] : 0.0;
+    const double r = e < n ? __ldcg(rates + e) : 0.0;
     __syncthreads();
     sc[t] = r;
     __syncthreads();
@@ -327,6 +301,47 @@ __global__ void __launch_bounds__(kPickThreads) k_rate_pick(const long long n, c
         }
         o.counters[0] = st + 1;
     }
+}
+
+// Rejection-free selection in one launch: block b computes rate_e =
+// exp(-beta dE_e / 2) for its kSelChunk entries (0 where masked), stores them and
+// their sum part[b] (fixed-order reduction); the last block to finish (ticket)
+// scans the partial sums and picks.  No block waits on another.
+__global__ void __launch_bounds__(kSelChunk) k_rate_select(const long long n, const int M,
+                                                           const double *__restrict__ diffs,
+                                                           const long long *__restrict__ masks, const double hb,
+                                                           double *part, double *rates, const double *__restrict__ ppos,
+                                                           const Key key, SelOut o, int *site_of, int *occ,
+                                                           const int *__restrict__ tsite, unsigned int *ticket)
+{
+    __shared__ double wsum[kSelChunk / 32];
+    __shared__ bool last;
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    const int nb = gridDim.x;
+    const long long e = (long long)blockIdx.x * kSelChunk + t;
+    const bool on = e < n && masks[e] > 0;
+    const double r = on ? exp(-hb * diffs[e]) : 0.0;
+    if (e < n) rates[e] = r;
+    __threadfence();
+    const int na = __syncthreads_count(on);
+    double x = r;
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+    if (lane == 0) wsum[wid] = x;
+    __syncthreads();
+    if (t == 0) {
+        double b = 0.0;
+        for (int w = 0; w < kSelChunk / 32; ++w) b += wsum[w];
+        part[blockIdx.x] = b;
+        atomicAdd((unsigned long long *)&o.counters[2], (unsigned long long)na);
+        __threadfence();
+        const unsigned int k = atomicAdd(ticket, 1u);
+        last = (k == (unsigned int)nb - 1);
+        if (last) *ticket = 0u;  // every block has taken its ticket: reset for the next step
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    rate_pick(n, nb, M, diffs, rates, part, ppos, key, o, site_of, occ, tsite);
 }
 
 // Metropolis on one uniformly chosen charge: accept its proposal with
@@ -369,6 +384,7 @@ struct kmc_driver {
     double *ppos = nullptr, *diffs = nullptr, *part = nullptr, *rates = nullptr;
     long long *masks = nullptr, *smc = nullptr, *sites = nullptr;
     int *tsite = nullptr, *site_of = nullptr, *occ = nullptr;
+    unsigned int *ticket = nullptr;  // selection blocks finished this step (k_rate_select)
     long long *sel_pid = nullptr, *counters = nullptr, *log_pid = nullptr, *log_tgt = nullptr;
     double *sel_pos = nullptr, *sel_de = nullptr, *log_de = nullptr;
     cudaGraph_t graph = nullptr;
@@ -393,8 +409,8 @@ int enqueue_step(kmc_driver *d, cudaStream_t st)
     const unsigned gb = (unsigned)((N + kGenThreads - 1) / kGenThreads);
     SelOut o{d->sel_pid, d->sel_pos, d->sel_de, d->counters, d->log_pid, d->log_tgt, d->log_de, d->prm.log_capacity};
     if (d->prm.kind == KMC_DRIVE_LATTICE)
-        k_lat_gen<<<gb, kGenThreads, 0, st>>>(N, d->side, d->spacing, half_e, d->wrap, d->site_of, d->occ, d->ppos,
-                                              d->masks, d->tsite);
+        k_lat_gen<<<(unsigned)((6 * (long long)N + kGenThreads - 1) / kGenThreads), kGenThreads, 0, st>>>(
+            N, d->side, d->spacing, half_e, d->wrap, d->site_of, d->occ, d->ppos, d->masks, d->tsite);
     else
         k_off_gen<<<gb, kGenThreads, 0, st>>>(N, half_e, d->prm.step, kmc_int_positions(d->sys), d->key,
                                               d->counters, d->ppos);
@@ -406,9 +422,8 @@ int enqueue_step(kmc_driver *d, cudaStream_t st)
         const long long n = (long long)N * d->M;
         const int nb = (int)((n + kSelChunk - 1) / kSelChunk);
         const double hb = 0.5 * d->prm.beta;
-        k_rate_partial<<<nb, kSelThreads, 0, st>>>(n, d->diffs, d->masks, hb, d->part, d->rates, d->counters);
-        k_rate_pick<<<1, kPickThreads, 0, st>>>(n, nb, d->M, d->diffs, d->rates, d->part, d->ppos, d->key, o,
-                                                d->site_of, d->occ, d->tsite);
+        k_rate_select<<<nb, kSelChunk, 0, st>>>(n, d->M, d->diffs, d->masks, hb, d->part, d->rates, d->ppos, d->key,
+                                                o, d->site_of, d->occ, d->tsite, d->ticket);
     } else {
         k_metropolis<<<1, 32, 0, st>>>(N, d->prm.beta, d->diffs, d->ppos, d->key, o);
     }
@@ -508,7 +523,7 @@ int kmc_driver_create(kmc_system *s, const kmc_driver_params *p, kmc_driver **ou
         !own(d, &d->smc, 1) ||
         !own(d, &d->sites, N) || !own(d, &d->part, nb) || !own(d, &d->sel_pid, 1) || !own(d, &d->sel_pos, 3) ||
         !own(d, &d->sel_de, 1) || !own(d, &d->counters, 3) || !own(d, &d->log_pid, lc) || !own(d, &d->log_tgt, lc) ||
-        !own(d, &d->log_de, lc)) {
+        !own(d, &d->log_de, lc) || !own(d, &d->ticket, 1)) {
         release(d);
         return KMC_ENOMEM;
     }
@@ -516,6 +531,7 @@ int kmc_driver_create(kmc_system *s, const kmc_driver_params *p, kmc_driver **ou
     bool ok = cudaMemcpy(d->smc, &smc, sizeof(long long), cudaMemcpyHostToDevice) == cudaSuccess &&
               cudaMemset(d->sites, 0, sizeof(long long) * N) == cudaSuccess &&
               cudaMemset(d->counters, 0, sizeof(long long) * 3) == cudaSuccess &&
+              cudaMemset(d->ticket, 0, sizeof(unsigned int)) == cudaSuccess &&
               cudaMemset(d->diffs, 0, sizeof(double) * nm) == cudaSuccess;
     if (ok && p->kind == KMC_DRIVE_OFFLATTICE) {
         k_fill_i64<<<(unsigned)((nm + 255) / 256), 256>>>(d->masks, (long long)nm, 1);

@@ -160,3 +160,79 @@ def test_mixed_kernel_variants(fused, groups):
     assert rel_err(g32.energy, g64.energy) < 1e-12
     g64.free()
     g32.free()
+
+
+@pytest.mark.parametrize("bc", ["free_space", "27", "pbc"])
+@pytest.mark.parametrize("R", [2, 3])
+def test_mixed_near_packed_and_scalar(bc, R):
+    """The near field summed two neighbours per packed FP32 instruction (default)
+    and one at a time give the same differences to double-FP32 rounding, and both
+    stay within the mixed tolerance of FP64.  Off-lattice charges give odd
+    neighbour counts (a padded pair) and, at R = 2 with periodic images, cells
+    that appear more than once in a neighbourhood."""
+    from coulomb_kmc_gb300 import _native
+    N, E, M = 300, 8.0, 3
+    rng = np.random.default_rng(11 + R)
+    P = rng.uniform(-0.5 * E, 0.5 * E, (N, 3))
+    Q = neutral_charges(N)
+    (g64, _), (g32, _) = both(P, Q, E, bc, R, 10)
+    smc = np.array([M], np.int64)
+    sites = np.zeros((N, 1), np.int64)
+    masks = rng.integers(0, 2, (N, M)).astype(np.int64)
+    ppos = np.clip(np.repeat(P, M, axis=0).reshape(N, 3 * M) + rng.uniform(-0.5, 0.5, (N, 3 * M)),
+                   -0.5 * E, 0.5 * E)
+    lib = _native.lib()
+    d64, dp, ds = np.zeros((N, M)), np.zeros((N, M)), np.zeros((N, M))
+    g64.propose_with_dats(smc, sites, ppos, masks, d64)
+    assert lib.kmc_set_tuning(g32._handle, 3, 0) == 0
+    g32.propose_with_dats(smc, sites, ppos, masks, dp)
+    assert lib.kmc_set_tuning(g32._handle, 3, 1) == 0
+    g32.propose_with_dats(smc, sites, ppos, masks, ds)
+    assert lib.kmc_set_tuning(g32._handle, 3, 2) != 0
+    assert lib.kmc_set_tuning(g32._handle, 4, 1) == 0
+    dc = np.zeros((N, M))
+    g32.propose_with_dats(smc, sites, ppos, masks, dc)
+    assert rel_err(dc[masks > 0], ds[masks > 0]).max() < 1e-11
+    act = masks > 0
+    assert rel_err(dp[act], ds[act]).max() < 1e-11
+    assert rel_err(dp[act], d64[act]).max() < MIXED_TOL
+    assert rel_err(ds[act], d64[act]).max() < MIXED_TOL
+    g64.free()
+    g32.free()
+
+
+def test_mixed_lattice_cache_through_accepts():
+    """The per-charge far-lattice cache (h = A b kept between moves, the accepted
+    charge's entry refreshed by the accept) gives the same differences as
+    recomputing h every propose (to FP32 rounding of b.g), through device-side
+    accepts, and both stay within the mixed tolerance of FP64."""
+    from coulomb_kmc_gb300 import _native
+    hs = LatticeHopSystem(side=16, occupancy=0.25, seed=9)
+    (g64, _), (g32, _) = both(hs.positions(), hs.charges(), hs.extent, "pbc", 3, 12, max_move=1.0)
+    lib = _native.lib()
+    rng = np.random.default_rng(4)
+    for _ in range(4):
+        ppos, masks, tsite = hs.proposals()
+        smc = np.array([6], np.int64)
+        sites = np.zeros((hs.n, 1), np.int64)
+        d64, dc, dn = np.zeros((hs.n, 6)), np.zeros((hs.n, 6)), np.zeros((hs.n, 6))
+        g64.propose_with_dats(smc, sites, ppos, masks, d64)
+        assert lib.kmc_set_tuning(g32._handle, 5, 0) == 0
+        g32.propose_with_dats(smc, sites, ppos, masks, dc)
+        assert lib.kmc_set_tuning(g32._handle, 5, 1) == 0
+        g32.propose_with_dats(smc, sites, ppos, masks, dn)
+        assert lib.kmc_set_tuning(g32._handle, 5, 0) == 0
+        act = masks > 0
+        # the two kernels sum the FP32 part of b.g (l >= 3) in different orders
+        assert rel_err(dc[act], dn[act]).max() < 1e-7
+        assert rel_err(dc[act], d64[act]).max() < MIXED_TOL
+        pid, h = hs.select(d64, masks, rng, 2.0)
+        mv = ppos[pid, 3 * h:3 * h + 3].copy()
+        g64.accept((pid, mv))
+        g32.accept_device(torch.tensor([pid], device="cuda"), torch.from_numpy(mv).cuda(),
+                          torch.zeros(1, dtype=torch.float64, device="cuda"))
+        hs.occ[hs.site_of[pid]] = -1
+        hs.occ[tsite[pid, h]] = pid
+        hs.site_of[pid] = tsite[pid, h]
+    g64.free()
+    g32.free()
