@@ -385,6 +385,8 @@ struct kmc_driver {
     long long *masks = nullptr, *smc = nullptr, *sites = nullptr;
     int *tsite = nullptr, *site_of = nullptr, *occ = nullptr;
     unsigned int *ticket = nullptr;  // selection blocks finished this step (k_rate_select)
+    bool prepared = false;           // proposals of the current state generated and set up
+    int64_t seen = -1;               // the system's launch count when they were
     long long *sel_pid = nullptr, *counters = nullptr, *log_pid = nullptr, *log_tgt = nullptr;
     double *sel_pos = nullptr, *sel_de = nullptr, *log_de = nullptr;
     cudaGraph_t graph = nullptr;
@@ -402,22 +404,50 @@ bool own(kmc_driver *d, T **p, size_t n)
     return true;
 }
 
-int enqueue_step(kmc_driver *d, cudaStream_t st)
+// Proposal generation and set-up for the next step on stream st: the hops (or
+// displacements) of the current state, compacted and grouped by target cell.
+int enqueue_prepare(kmc_driver *d, cudaStream_t st)
 {
     const int N = d->N;
     const double half_e = 0.5 * d->E;
-    const unsigned gb = (unsigned)((N + kGenThreads - 1) / kGenThreads);
-    SelOut o{d->sel_pid, d->sel_pos, d->sel_de, d->counters, d->log_pid, d->log_tgt, d->log_de, d->prm.log_capacity};
     if (d->prm.kind == KMC_DRIVE_LATTICE)
         k_lat_gen<<<(unsigned)((6 * (long long)N + kGenThreads - 1) / kGenThreads), kGenThreads, 0, st>>>(
             N, d->side, d->spacing, half_e, d->wrap, d->site_of, d->occ, d->ppos, d->masks, d->tsite);
     else
-        k_off_gen<<<gb, kGenThreads, 0, st>>>(N, half_e, d->prm.step, kmc_int_positions(d->sys), d->key,
-                                              d->counters, d->ppos);
+        k_off_gen<<<(unsigned)((N + kGenThreads - 1) / kGenThreads), kGenThreads, 0, st>>>(
+            N, half_e, d->prm.step, kmc_int_positions(d->sys), d->key, d->counters, d->ppos);
     if (cudaGetLastError() != cudaSuccess) return KMC_ECUDA;
-    int rc = kmc_propose_with_dats(d->sys, N, d->M, 1, (const int64_t *)d->smc, (const int64_t *)d->sites, d->ppos,
-                                   (const int64_t *)d->masks, nullptr, d->diffs);
+    return kmc_int_propose_prepare(d->sys, (void *)st, N, d->M, (const int64_t *)d->smc, (const int64_t *)d->sites,
+                                   d->ppos, (const int64_t *)d->masks);
+}
+
+int prepare_branch(void *ctx, void *stream) { return enqueue_prepare((kmc_driver *)ctx, (cudaStream_t)stream); }
+
+// before a graph replay or capture: the replayed step expects prepared proposals
+int ensure_prepared(kmc_driver *d, cudaStream_t st)
+{
+    if (d->prepared && d->seen == kmc_int_launches(d->sys)) return KMC_OK;
+    const int rc = enqueue_prepare(d, st);
     if (rc) return rc;
+    d->prepared = true;
+    d->seen = kmc_int_launches(d->sys);
+    return KMC_OK;
+}
+
+// One step, software-pipelined: the proposals of this step were prepared at the
+// end of the previous one (or are prepared here when anything else has launched
+// work on the system since); evaluate, select, then accept with the next step's
+// generation and set-up beside the accept's expansion updates.  Every kernel
+// sees the same inputs as in the plain order generate -> propose -> select ->
+// accept, so the results are the same.
+int enqueue_step(kmc_driver *d, cudaStream_t st)
+{
+    const int N = d->N;
+    SelOut o{d->sel_pid, d->sel_pos, d->sel_de, d->counters, d->log_pid, d->log_tgt, d->log_de, d->prm.log_capacity};
+    int rc;
+    if (!d->prepared || d->seen != kmc_int_launches(d->sys))
+        if ((rc = enqueue_prepare(d, st))) return rc;
+    if ((rc = kmc_int_propose_evaluate(d->sys, N, d->M, d->diffs))) return rc;
     if (d->prm.kind == KMC_DRIVE_LATTICE) {
         const long long n = (long long)N * d->M;
         const int nb = (int)((n + kSelChunk - 1) / kSelChunk);
@@ -428,7 +458,13 @@ int enqueue_step(kmc_driver *d, cudaStream_t st)
         k_metropolis<<<1, 32, 0, st>>>(N, d->prm.beta, d->diffs, d->ppos, d->key, o);
     }
     if (cudaGetLastError() != cudaSuccess) return KMC_ECUDA;
-    return kmc_accept_device(d->sys, (const int64_t *)d->sel_pid, d->sel_pos, d->sel_de);
+    d->prepared = false;
+    if ((rc = kmc_int_accept_device_branch(d->sys, (const int64_t *)d->sel_pid, d->sel_pos, d->sel_de,
+                                           prepare_branch, d)))
+        return rc;
+    d->prepared = true;
+    d->seen = kmc_int_launches(d->sys);
+    return KMC_OK;
 }
 
 void release(kmc_driver *d)
@@ -574,13 +610,16 @@ int kmc_driver_capture(kmc_driver *d)
         cudaGraphDestroy(d->graph);
         d->graph = nullptr;
     }
+    int rc = ensure_prepared(d, st);
+    if (rc) return rc;
     if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return KMC_ECUDA;
-    const int rc = enqueue_step(d, st);
+    rc = enqueue_step(d, st);
     cudaGraph_t g = nullptr;
     const cudaError_t e = cudaStreamEndCapture(st, &g);
     if (rc || e != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
         cudaGetLastError();
+        d->prepared = false;
         return rc ? rc : KMC_ECUDA;
     }
     d->graph = g;
@@ -593,6 +632,8 @@ int kmc_driver_launch(kmc_driver *d, int64_t nsteps, void *stream)
     if (!d || nsteps < 0) return KMC_EINVAL;
     if (!d->exec) return KMC_ESTATE;
     cudaStream_t st = stream ? (cudaStream_t)stream : kmc_int_stream(d->sys);
+    int rc = ensure_prepared(d, st);
+    if (rc) return rc;
     for (int64_t k = 0; k < nsteps; ++k)
         if (cudaGraphLaunch(d->exec, st) != cudaSuccess) return KMC_ECUDA;
     return KMC_OK;
@@ -675,6 +716,10 @@ int kmc_drivers_launch(kmc_driver **drivers, int64_t n, int64_t steps, void *mai
     const int64_t nw = n_workers < n ? n_workers : n;
     for (int64_t w = 0; w < nw; ++w)
         if (cudaStreamWaitEvent((cudaStream_t)worker_streams[w], ev[0], 0) != cudaSuccess) return KMC_ECUDA;
+    for (int64_t i = 0; i < n; ++i) {
+        const int rc = ensure_prepared(drivers[i], (cudaStream_t)worker_streams[i % nw]);
+        if (rc) return rc;
+    }
     for (int64_t k = 0; k < steps; ++k)
         for (int64_t i = 0; i < n; ++i)
             if (cudaGraphLaunch(drivers[i]->exec, (cudaStream_t)worker_streams[i % nw]) != cudaSuccess)

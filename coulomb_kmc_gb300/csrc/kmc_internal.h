@@ -18,5 +18,16 @@ const double *kmc_int_positions(const kmc_system *s);  // device [N][3], updated
 // later stream capture of propose + accept needs no allocation
 int kmc_int_reserve(kmc_system *s, int64_t n, int64_t nm);
 bool kmc_int_initialised(const kmc_system *s);
+// kmc_propose_with_dats in two parts: the proposal set-up (compaction, cell
+// sort) on a given stream, and the evaluation on the system's stream
+int kmc_int_propose_prepare(kmc_system *s, void *stream, int64_t n, int64_t max_prop, const int64_t *site_max_counts,
+                            const int64_t *current_sites, const double *prop_positions, const int64_t *prop_masks);
+int kmc_int_propose_evaluate(kmc_system *s, int64_t n, int64_t max_prop, double *prop_energy_diffs);
+// kmc_accept_device with the caller's work (branch) enqueued on a stream that
+// forks after the store / position update and joins with the accept's end
+int kmc_int_accept_device_branch(kmc_system *s, const int64_t *d_pid, const double *d_new_position,
+                                 const double *d_energy_diff, int (*branch)(void *ctx, void *stream), void *ctx);
+// launches made on the system so far (host count; graph replays add none)
+int64_t kmc_int_launches(const kmc_system *s);
 
 } // extern "C"
