@@ -623,9 +623,8 @@ def main():
         t0 = time.perf_counter()
         n2 = 0
         for _ in range(args.e2e_steps):
-            _, m2, _ = e2e_sys.proposals()
-            n2 += int(m2.sum())
             e2e_sys.step(k2, rng, BETA)
+            n2 += e2e_sys.last_active
         torch.cuda.synchronize()
         e2e_dt = time.perf_counter() - t0
         n = e2e_sys.n

@@ -387,6 +387,7 @@ struct kmc_driver {
     unsigned int *ticket = nullptr;  // selection blocks finished this step (k_rate_select)
     bool prepared = false;           // proposals of the current state generated and set up
     int64_t seen = -1;               // the system's launch count when they were
+    bool graph_pipelined = false;    // the captured step is the pipelined form
     long long *sel_pid = nullptr, *counters = nullptr, *log_pid = nullptr, *log_tgt = nullptr;
     double *sel_pos = nullptr, *sel_de = nullptr, *log_de = nullptr;
     cudaGraph_t graph = nullptr;
@@ -423,7 +424,17 @@ int enqueue_prepare(kmc_driver *d, cudaStream_t st)
 
 int prepare_branch(void *ctx, void *stream) { return enqueue_prepare((kmc_driver *)ctx, (cudaStream_t)stream); }
 
-// before a graph replay or capture: the replayed step expects prepared proposals
+// Pipelined steps (the default beside the double-FP32 accept): the next step's
+// set-up runs beside the accept.  Plain order for FP64 accepts, whose
+// particle-to-local blocks fill whole SMs with shared memory: set-up kernels
+// interleaved with them delay them (0.73 -> 0.95 ms per step on the 48^3
+// lattice), while beside the double-FP32 accept they hide (0.38 -> 0.31 ms).
+bool pipelined(const kmc_driver *d)
+{
+    return kmc_int_tuning(d->sys, KMC_TUNE_DRIVER_SERIAL) != 1 && kmc_int_accept_df32(d->sys);
+}
+
+// before a replay or capture of a pipelined step: it expects prepared proposals
 int ensure_prepared(kmc_driver *d, cudaStream_t st)
 {
     if (d->prepared && d->seen == kmc_int_launches(d->sys)) return KMC_OK;
@@ -445,7 +456,8 @@ int enqueue_step(kmc_driver *d, cudaStream_t st)
     const int N = d->N;
     SelOut o{d->sel_pid, d->sel_pos, d->sel_de, d->counters, d->log_pid, d->log_tgt, d->log_de, d->prm.log_capacity};
     int rc;
-    if (!d->prepared || d->seen != kmc_int_launches(d->sys))
+    const bool pipe = pipelined(d);
+    if (!pipe || !d->prepared || d->seen != kmc_int_launches(d->sys))
         if ((rc = enqueue_prepare(d, st))) return rc;
     if ((rc = kmc_int_propose_evaluate(d->sys, N, d->M, d->diffs))) return rc;
     if (d->prm.kind == KMC_DRIVE_LATTICE) {
@@ -459,6 +471,10 @@ int enqueue_step(kmc_driver *d, cudaStream_t st)
     }
     if (cudaGetLastError() != cudaSuccess) return KMC_ECUDA;
     d->prepared = false;
+    if (!pipe) {
+        // plain order: the next step prepares at its start
+        return kmc_accept_device(d->sys, (const int64_t *)d->sel_pid, d->sel_pos, d->sel_de);
+    }
     if ((rc = kmc_int_accept_device_branch(d->sys, (const int64_t *)d->sel_pid, d->sel_pos, d->sel_de,
                                            prepare_branch, d)))
         return rc;
@@ -513,9 +529,9 @@ int kmc_driver_create(kmc_system *s, const kmc_driver_params *p, kmc_driver **ou
         const long long nsites = (long long)d->side * d->side * d->side;
         std::vector<int> occ((size_t)nsites, -1), so(N);
         std::vector<double> pos(3 * (size_t)N);
-        if (cudaStreamSynchronize(st) != cudaSuccess ||
-            cudaMemcpy(pos.data(), kmc_int_positions(s), sizeof(double) * pos.size(), cudaMemcpyDeviceToHost) !=
-                cudaSuccess) {
+        if (cudaMemcpyAsync(pos.data(), kmc_int_positions(s), sizeof(double) * pos.size(), cudaMemcpyDeviceToHost,
+                            st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) {
             delete d;
             return KMC_ECUDA;
         }
@@ -540,8 +556,10 @@ int kmc_driver_create(kmc_system *s, const kmc_driver_params *p, kmc_driver **ou
             release(d);
             return KMC_ENOMEM;
         }
-        if (cudaMemcpy(d->site_of, so.data(), sizeof(int) * N, cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(d->occ, occ.data(), sizeof(int) * occ.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        if (cudaMemcpyAsync(d->site_of, so.data(), sizeof(int) * N, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+            cudaMemcpyAsync(d->occ, occ.data(), sizeof(int) * occ.size(), cudaMemcpyHostToDevice, st) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) {
             release(d);
             return KMC_ECUDA;
         }
@@ -563,16 +581,20 @@ int kmc_driver_create(kmc_system *s, const kmc_driver_params *p, kmc_driver **ou
         release(d);
         return KMC_ENOMEM;
     }
+    // stream-ordered on the system's stream only: other threads may be capturing
+    // graphs of other systems meanwhile, so nothing here touches the legacy stream
+    // or synchronises the device
     const long long smc = d->M;
-    bool ok = cudaMemcpy(d->smc, &smc, sizeof(long long), cudaMemcpyHostToDevice) == cudaSuccess &&
-              cudaMemset(d->sites, 0, sizeof(long long) * N) == cudaSuccess &&
-              cudaMemset(d->counters, 0, sizeof(long long) * 3) == cudaSuccess &&
-              cudaMemset(d->ticket, 0, sizeof(unsigned int)) == cudaSuccess &&
-              cudaMemset(d->diffs, 0, sizeof(double) * nm) == cudaSuccess;
+    bool ok = cudaMemcpyAsync(d->smc, &smc, sizeof(long long), cudaMemcpyHostToDevice, st) == cudaSuccess &&
+              cudaMemsetAsync(d->sites, 0, sizeof(long long) * N, st) == cudaSuccess &&
+              cudaMemsetAsync(d->counters, 0, sizeof(long long) * 3, st) == cudaSuccess &&
+              cudaMemsetAsync(d->ticket, 0, sizeof(unsigned int), st) == cudaSuccess &&
+              cudaMemsetAsync(d->diffs, 0, sizeof(double) * nm, st) == cudaSuccess;
     if (ok && p->kind == KMC_DRIVE_OFFLATTICE) {
-        k_fill_i64<<<(unsigned)((nm + 255) / 256), 256>>>(d->masks, (long long)nm, 1);
-        ok = cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess;
+        k_fill_i64<<<(unsigned)((nm + 255) / 256), 256, 0, st>>>(d->masks, (long long)nm, 1);
+        ok = cudaGetLastError() == cudaSuccess;
     }
+    ok = ok && cudaStreamSynchronize(st) == cudaSuccess;
     if (!ok) {
         release(d);
         return KMC_ECUDA;
@@ -610,7 +632,8 @@ int kmc_driver_capture(kmc_driver *d)
         cudaGraphDestroy(d->graph);
         d->graph = nullptr;
     }
-    int rc = ensure_prepared(d, st);
+    d->graph_pipelined = pipelined(d);
+    int rc = d->graph_pipelined ? ensure_prepared(d, st) : KMC_OK;
     if (rc) return rc;
     if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return KMC_ECUDA;
     rc = enqueue_step(d, st);
@@ -632,7 +655,7 @@ int kmc_driver_launch(kmc_driver *d, int64_t nsteps, void *stream)
     if (!d || nsteps < 0) return KMC_EINVAL;
     if (!d->exec) return KMC_ESTATE;
     cudaStream_t st = stream ? (cudaStream_t)stream : kmc_int_stream(d->sys);
-    int rc = ensure_prepared(d, st);
+    int rc = d->graph_pipelined ? ensure_prepared(d, st) : KMC_OK;
     if (rc) return rc;
     for (int64_t k = 0; k < nsteps; ++k)
         if (cudaGraphLaunch(d->exec, st) != cudaSuccess) return KMC_ECUDA;
@@ -717,7 +740,9 @@ int kmc_drivers_launch(kmc_driver **drivers, int64_t n, int64_t steps, void *mai
     for (int64_t w = 0; w < nw; ++w)
         if (cudaStreamWaitEvent((cudaStream_t)worker_streams[w], ev[0], 0) != cudaSuccess) return KMC_ECUDA;
     for (int64_t i = 0; i < n; ++i) {
-        const int rc = ensure_prepared(drivers[i], (cudaStream_t)worker_streams[i % nw]);
+        const int rc = drivers[i]->graph_pipelined
+                           ? ensure_prepared(drivers[i], (cudaStream_t)worker_streams[i % nw])
+                           : KMC_OK;
         if (rc) return rc;
     }
     for (int64_t k = 0; k < steps; ++k)

@@ -29,5 +29,7 @@ int kmc_int_accept_device_branch(kmc_system *s, const int64_t *d_pid, const doub
                                  const double *d_energy_diff, int (*branch)(void *ctx, void *stream), void *ctx);
 // launches made on the system so far (host count; graph replays add none)
 int64_t kmc_int_launches(const kmc_system *s);
+int kmc_int_tuning(const kmc_system *s, int key);
+bool kmc_int_accept_df32(const kmc_system *s);  // accept contributions in double-FP32 (precision mixed)
 
 } // extern "C"

@@ -33,6 +33,12 @@ class LatticeHopSystem:
         self.occ = np.full(nsites, -1, dtype=np.int64)
         self.occ[self.site_of] = np.arange(n)
         self.M = 6
+        # per site: the six neighbour sites in HOPS order (periodic) and every site's centre
+        xyz = self.site_xyz(np.arange(nsites))
+        tgt = (xyz[:, None, :] + HOPS[None, :, :]) % self.side
+        self._nb = tgt[..., 0] + self.side * (tgt[..., 1] + self.side * tgt[..., 2])
+        self._centre = xyz.astype(np.float64) - 0.5 * self.extent + 0.5
+        self.last_active = 0
 
     def site_xyz(self, s):
         s = np.asarray(s, dtype=np.int64)
@@ -51,12 +57,9 @@ class LatticeHopSystem:
 
     def proposals(self):
         """(prop_positions [n, 18], prop_masks [n, 6], target sites [n, 6])."""
-        k = self.side
-        xyz = self.site_xyz(self.site_of)
-        tgt = (xyz[:, None, :] + HOPS[None, :, :]) % k
-        tsite = tgt[..., 0] + k * (tgt[..., 1] + k * tgt[..., 2])
+        tsite = self._nb[self.site_of]
         masks = (self.occ[tsite] < 0).astype(np.int64)
-        ppos = (tgt.astype(np.float64) - 0.5 * self.extent + 0.5).reshape(self.n, 3 * self.M)
+        ppos = self._centre[tsite].reshape(self.n, 3 * self.M)
         return ppos, masks, tsite
 
     def select(self, diffs, masks, rng, beta):
@@ -75,6 +78,7 @@ class LatticeHopSystem:
         smc = np.array([self.M], dtype=np.int64)
         sites = np.zeros((self.n, 1), dtype=np.int64)
         kmc.propose_with_dats(smc, sites, ppos, masks, diffs)
+        self.last_active = int(masks.sum())
         pid, h = self.select(diffs, masks, rng, beta)
         newp = ppos[pid, 3 * h:3 * h + 3].copy()
         kmc.accept((pid, newp))
