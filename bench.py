@@ -132,7 +132,9 @@ def flop_model(kmc, host_sys, lr_nnz_folded):
     near_new = float(np.sum(11 * nb[pcell])) + nprop * (far + 27 * 11 + 4)
     near_old = float(np.sum(11 * nb[st["cells"][movers]])) + len(movers) * (far + 2)
     lr_new = nprop * (mpole + 4 * nh + lr_nnz_folded + 6)   # a, a.(g-h), a^T U a
-    lr_old = len(movers) * (mpole + 2 * 2 * lr_nnz_folded + 8 * nh)
+    # old side with h = A b kept per charge (mixed path): b and b.g per moving charge;
+    # the FP64 path recomputes h every step
+    lr_old = len(movers) * (mpole + 4 * nh + (0 if kmc.precision != "fp64" else 2 * 2 * lr_nnz_folded + 4 * nh))
     ncell = n ** 3
     p2l = ncell * 54 * (12 * nh + 6 * L + 15)
     return {"near_far_cell": near_new + near_old, "far_lattice": lr_new, "far_lattice_old": lr_old,
@@ -143,12 +145,12 @@ def flop_model(kmc, host_sys, lr_nnz_folded):
 # profiles/fp64_step_lattice48_launch_list.md (dram__bytes_read.sum + dram__bytes_write.sum)
 NCU_TRAFFIC = {"near_far_cell": 12.921088e6}
 # mixed path: profiles/k_near_cell_mixed_lattice48.md, k_p2l_df2_lattice48.md, k_lr_mixed_lattice48.md
-NCU_TRAFFIC_MIXED = {"near_far_cell": 13.074688e6, "accept_p2l": 5.233408e6, "far_lattice": 24.304384e6,
-                     "far_lattice_old": 1.036032e6}
+NCU_TRAFFIC_MIXED = {"near_far_cell": 12.643584e6, "accept_p2l": 5.235456e6, "far_lattice": 22.0992e6,
+                     "far_lattice_old": 1.241088e6}
 # warp instructions per launch from the same ncu capture (smsp__inst_executed.sum), for the
 # issue-slot fraction of the mixed kernels (4 warp instructions per SM per clock)
-NCU_INST_MIXED = {"near_far_cell": 115.812643e6, "accept_p2l": 78.166604e6, "far_lattice": 26.509679e6,
-                  "far_lattice_old": 17.393185e6}
+NCU_INST_MIXED = {"near_far_cell": 80.755949e6, "accept_p2l": 39.863372e6, "far_lattice": 27.225926e6,
+                  "far_lattice_old": 2.839752e6}
 
 
 def issue_fracs(per_launch_ms, clk):
@@ -450,6 +452,62 @@ def bench_batched(args):
     print(json.dumps(line))
 
 
+def bench_drift(args):
+    """Mixed vs FP64 after long chains of accepts on the 48^3 lattice: the mixed
+    driver runs and logs its selections, the same moves are accepted on an FP64
+    system, then both evaluate the proposals of the common state."""
+    import torch
+    from coulomb_kmc_gb300 import KMCFMM, _native
+    from coulomb_kmc_gb300.dats import make_state
+    from coulomb_kmc_gb300.driver import KMCDriver
+    from coulomb_kmc_gb300.workloads import LatticeHopSystem
+    hs = LatticeHopSystem(SIDE, OCC, seed=1)
+    ks = {}
+    for prec in ("fp64", "mixed"):
+        st = make_state(hs.positions(), hs.charges(), hs.extent)
+        ks[prec] = KMCFMM(st.P, st.Q, st.domain, r=R, l=L, boundary_condition="pbc", max_move=1.0, precision=prec)
+        ks[prec].initialise()
+    if args.fp32_from is not None:
+        assert _native.lib().kmc_set_tuning(ks["mixed"]._handle, 6, args.fp32_from) == 0
+    chunk = 10000
+    drv = KMCDriver(ks["mixed"], "lattice", BETA, seed=77, lattice_side=hs.side, lattice_sites=hs.site_of,
+                    log_capacity=chunk)
+    out, done = [], 0
+    for target in args.accepts:
+        while done < target:
+            k = min(chunk, target - done)
+            drv.step(k)
+            torch.cuda.synchronize()
+            pid, tgt, _ = drv.log()
+            for p_, t_ in zip(pid[-k:], tgt[-k:]):
+                if p_ < 0:
+                    continue
+                ks["fp64"].accept((int(p_), hs.site_pos(int(t_))))
+                hs.occ[hs.site_of[p_]] = -1
+                hs.occ[t_] = p_
+                hs.site_of[p_] = t_
+            done += k
+        assert np.array_equal(drv.sites(), hs.site_of)
+        ppos, masks, _ = hs.proposals()
+        smc = np.array([6], np.int64)
+        sites = np.zeros((hs.n, 1), np.int64)
+        d = {}
+        for prec, kk in ks.items():
+            d[prec] = np.zeros((hs.n, 6))
+            kk.propose_with_dats(smc, sites, ppos, masks, d[prec])
+        act = masks > 0
+        e = np.abs(d["mixed"][act] - d["fp64"][act]) / np.maximum(np.abs(d["fp64"][act]), 1.0)
+        le = np.max(np.abs(ks["mixed"].state()["local_expansions"] - ks["fp64"].state()["local_expansions"]))
+        out.append({"accepts": done, "max_rel": float(e.max()), "rms_rel": float(np.sqrt(np.mean(e * e))),
+                    "energy_rel": abs(ks["mixed"].energy - ks["fp64"].energy) / abs(ks["fp64"].energy),
+                    "expansions_max_abs_diff": float(le)})
+    drv.free()
+    for kk in ks.values():
+        kk.free()
+    print(json.dumps({"workload": "drift", "config": {"workload": "pbc lattice-hop 48^3 sites, mixed driver "
+                      "selections replayed on FP64", "fp32_from": args.fp32_from}, "results": out}))
+
+
 def bench_serving(args):
     """Poisson request stream through the continuous-batching server."""
     from coulomb_kmc_gb300.serving import Server, one_at_a_time, poisson_requests
@@ -494,7 +552,10 @@ def main():
     ap.add_argument("--ref-steps", type=int, default=10)
     ap.add_argument("--no-extras", action="store_true", help="timed loop only (for profiler runs)")
     ap.add_argument("--no-graph", action="store_true", help="launch the step eagerly instead of a CUDA graph")
-    ap.add_argument("--workload", default="lattice48", choices=["lattice48", "precision_split", "batched", "serving"])
+    ap.add_argument("--workload", default="lattice48",
+                    choices=["lattice48", "precision_split", "batched", "serving", "drift"])
+    ap.add_argument("--accepts", type=int, nargs="+", default=[0, 2000, 10000, 30000])
+    ap.add_argument("--fp32-from", type=int, default=None, help="drift: first accept order in FP32 (tuning key 6)")
     ap.add_argument("--orders", type=int, nargs="+", default=[8, 12, 16])
     ap.add_argument("--error-steps", type=int, default=3)
     ap.add_argument("--systems", type=int, default=64)
@@ -510,7 +571,8 @@ def main():
     if args.workload != "lattice48" and args.impl == "ours":
         import torch
         torch.cuda.set_device(0)
-        {"precision_split": bench_precision_split, "batched": bench_batched, "serving": bench_serving}[
+        {"precision_split": bench_precision_split, "batched": bench_batched, "serving": bench_serving,
+         "drift": bench_drift}[
             args.workload](args)
         return
 
