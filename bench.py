@@ -225,9 +225,8 @@ def cpu_reference(steps, warmup, side, with_gpu_state=None):
     t0 = time.perf_counter()
     nprop = 0
     for _ in range(steps):
-        _, masks, _ = hs.proposals()
-        nprop += int(masks.sum())
         hs.step(o, rng, BETA)
+        nprop += hs.last_active
     dt = time.perf_counter() - t0
     return nprop / dt, dt, nprop
 

@@ -89,6 +89,7 @@ SIGNATURES = {
     "kmc_info": ([c_void_p, POINTER(c_int64), POINTER(c_int64), POINTER(c_int64)], c_int),
     "kmc_profile": ([c_void_p, c_int32], c_int),
     "kmc_profile_read": ([c_void_p, c_int32, c_void_p, c_void_p, POINTER(c_int64)], c_int),
+    "kmc_profile_timeline": ([c_void_p, c_int64, c_void_p, c_void_p, c_void_p, POINTER(c_int64)], c_int),
     "kmc_kernel_name": ([c_int32], c_char_p),
     "kmc_eval_field": ([c_void_p, c_int64, c_void_p, c_void_p], c_int),
     "kmc_get_energy_ids": ([c_void_p, c_int64, c_void_p, c_void_p], c_int),

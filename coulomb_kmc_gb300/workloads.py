@@ -39,6 +39,7 @@ class LatticeHopSystem:
         self._nb = tgt[..., 0] + self.side * (tgt[..., 1] + self.side * tgt[..., 2])
         self._centre = xyz.astype(np.float64) - 0.5 * self.extent + 0.5
         self.last_active = 0
+        self._cache = None  # step(): [ppos, masks, tsite, site_of copy], updated per accepted hop
 
     def site_xyz(self, s):
         s = np.asarray(s, dtype=np.int64)
@@ -62,8 +63,40 @@ class LatticeHopSystem:
         ppos = self._centre[tsite].reshape(self.n, 3 * self.M)
         return ppos, masks, tsite
 
+    def _step_proposals(self):
+        """proposals() kept current across step()'s own accepts (one hop changes one
+        charge's targets and the masks of the two sites' neighbours); rebuilt when
+        anything else changed the occupancy."""
+        c = self._cache
+        if c is None or not np.array_equal(c[3], self.site_of):
+            ppos, masks, tsite = self.proposals()
+            self._cache = c = [ppos, masks, tsite, self.site_of.copy()]
+        return c[0], c[1], c[2]
+
+    def _commit(self, pid, old, new):
+        self.occ[old] = -1
+        self.occ[new] = pid
+        self.site_of[pid] = new
+        c = self._cache
+        if c is None:
+            return
+        ppos, masks, tsite, sites = c
+        for h in range(self.M):  # hop h ^ 1 of the charge at nb[s][h] leads back to s
+            j = self.occ[self._nb[old, h]]
+            if j >= 0:
+                masks[j, h ^ 1] = 1
+            j = self.occ[self._nb[new, h]]
+            if j >= 0:
+                masks[j, h ^ 1] = 0
+        t = self._nb[new]
+        tsite[pid] = t
+        masks[pid] = self.occ[t] < 0
+        ppos[pid] = self._centre[t].reshape(-1)
+        sites[pid] = new
+
     def select(self, diffs, masks, rng, beta):
-        rates = np.where(masks > 0, np.exp(-0.5 * beta * diffs), 0.0).ravel()
+        rates = np.zeros(masks.size)
+        np.exp(-0.5 * beta * diffs.ravel(), out=rates, where=masks.ravel() > 0)
         c = np.cumsum(rates)
         u = rng.uniform(0.0, c[-1])
         idx = int(np.searchsorted(c, u, side="right"))
@@ -73,7 +106,7 @@ class LatticeHopSystem:
         return idx // self.M, idx % self.M
 
     def step(self, kmc, rng, beta=2.0):
-        ppos, masks, tsite = self.proposals()
+        ppos, masks, tsite = self._step_proposals()
         diffs = np.zeros((self.n, self.M))
         smc = np.array([self.M], dtype=np.int64)
         sites = np.zeros((self.n, 1), dtype=np.int64)
@@ -82,12 +115,9 @@ class LatticeHopSystem:
         pid, h = self.select(diffs, masks, rng, beta)
         newp = ppos[pid, 3 * h:3 * h + 3].copy()
         kmc.accept((pid, newp))
-        old = self.site_of[pid]
-        new = tsite[pid, h]
-        self.occ[old] = -1
-        self.occ[new] = pid
-        self.site_of[pid] = new
-        return int(pid), int(new)
+        old, new = int(self.site_of[pid]), int(tsite[pid, h])
+        self._commit(pid, old, new)
+        return int(pid), new
 
 
 class OffLatticeSystem:

@@ -168,6 +168,13 @@ int kmc_info(kmc_system *s, int64_t *ncell, int64_t *capacity, int64_t *n);
 #define KMC_NKERNELS 18
 int kmc_profile(kmc_system *s, int32_t enable);
 int kmc_profile_read(kmc_system *s, int32_t reset, double *ms_out, int64_t *count_out, int64_t *launches_out);
+/* Diagnostics, no reference counterpart: the launches bracketed since the last
+ * read, in launch order, with start and end times (ms, CUDA events) relative to
+ * the first one's start, so that concurrent streams show as overlaps.  Consumes
+ * them like kmc_profile_read (their durations are added to its totals);
+ * synchronises the device. */
+int kmc_profile_timeline(kmc_system *s, int64_t max_entries, int32_t *ids_out, double *start_ms, double *end_ms,
+                         int64_t *n_out);
 const char *kmc_kernel_name(int32_t id);
 
 /* Potential of all charges at n points (device arrays [n][3] and [n]), without
