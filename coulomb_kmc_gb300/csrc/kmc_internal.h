@@ -19,7 +19,10 @@ const double *kmc_int_positions(const kmc_system *s);  // device [N][3], updated
 int kmc_int_reserve(kmc_system *s, int64_t n, int64_t nm);
 bool kmc_int_initialised(const kmc_system *s);
 // kmc_propose_with_dats in two parts: the proposal set-up (compaction, cell
-// sort) on a given stream, and the evaluation on the system's stream
+// sort) on a given stream, and the evaluation on the system's stream.  The
+// set-up skips the per-move checks: it serves the device driver, whose moves are
+// valid by construction (spacing / step <= max_move checked at creation,
+// positions inside the box)
 int kmc_int_propose_prepare(kmc_system *s, void *stream, int64_t n, int64_t max_prop, const int64_t *site_max_counts,
                             const int64_t *current_sites, const double *prop_positions, const int64_t *prop_masks);
 int kmc_int_propose_evaluate(kmc_system *s, int64_t n, int64_t max_prop, double *prop_energy_diffs);
