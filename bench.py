@@ -559,7 +559,7 @@ def main():
     ap.add_argument("--error-steps", type=int, default=3)
     ap.add_argument("--systems", type=int, default=64)
     ap.add_argument("--rounds", type=int, default=20)
-    ap.add_argument("--workers", type=int, default=8)
+    ap.add_argument("--workers", type=int, default=16)
     ap.add_argument("--requests", type=int, default=16)
     ap.add_argument("--rates", type=float, nargs="+", default=[50.0, 2000.0])
     ap.add_argument("--max-n", type=int, default=262144)

@@ -127,7 +127,7 @@ class _null:
 
 
 class Server:
-    def __init__(self, precision="mixed", hbm_budget=150e9, max_active=64, n_workers=8, keep_results=False,
+    def __init__(self, precision="mixed", hbm_budget=150e9, max_active=64, n_workers=16, keep_results=False,
                  n_admit=4):
         import torch
         self.precision = precision
