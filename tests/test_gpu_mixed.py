@@ -242,3 +242,30 @@ def test_mixed_lattice_cache_through_accepts():
         hs.site_of[pid] = tsite[pid, h]
     g64.free()
     g32.free()
+
+
+@pytest.mark.parametrize("bc", ["free_space", "pbc"])
+def test_mixed_shared_targets(bc):
+    """Many proposals to the same positions (the near field and cell expansion are
+    computed once per distinct position in a cell, the self term per proposal):
+    within the mixed tolerance of FP64, and a charge's two proposals to one
+    position give identical differences."""
+    N, E, M = 300, 8.0, 4
+    rng = np.random.default_rng(21)
+    P = rng.uniform(-0.5 * E, 0.5 * E, (N, 3))
+    Q = neutral_charges(N)
+    (g64, _), (g32, _) = both(P, Q, E, bc, 3, 12)
+    pool = rng.uniform(-0.5 * E, 0.5 * E, (40, 3))
+    pick = rng.integers(0, len(pool), (N, M))
+    pick[:, 1] = pick[:, 0]  # a duplicate within each charge's own moves
+    ppos = pool[pick].reshape(N, 3 * M)
+    masks = np.ones((N, M), np.int64)
+    smc = np.array([M], np.int64)
+    sites = np.zeros((N, 1), np.int64)
+    d64, d32 = np.zeros((N, M)), np.zeros((N, M))
+    g64.propose_with_dats(smc, sites, ppos, masks, d64)
+    g32.propose_with_dats(smc, sites, ppos, masks, d32)
+    assert rel_err(d32, d64).max() < MIXED_TOL
+    assert np.array_equal(d32[:, 0], d32[:, 1])
+    g64.free()
+    g32.free()
