@@ -244,6 +244,35 @@ def test_mixed_lattice_cache_through_accepts():
     g32.free()
 
 
+@pytest.mark.parametrize("side,cached", [(16, 0), (16, 1), (10, 0)])
+def test_mixed_self_term_evaluators(side, cached):
+    """The unrolled L = 12 cubic-lattice evaluator of the far-lattice self term F(x)
+    and the general program interpreter agree to FP32 rounding (a different
+    evaluation order, so not bit-identical), with and without the per-charge
+    lattice cache, and both stay within the mixed tolerance of FP64."""
+    from coulomb_kmc_gb300 import _native
+    hs = LatticeHopSystem(side=side, occupancy=0.25, seed=5)
+    (g64, _), (g32, _) = both(hs.positions(), hs.charges(), hs.extent, "pbc", 3, 12, max_move=1.0)
+    lib = _native.lib()
+    assert lib.kmc_set_tuning(g32._handle, 5, 1 - cached) == 0
+    ppos, masks, _ = hs.proposals()
+    smc = np.array([6], np.int64)
+    sites = np.zeros((hs.n, 1), np.int64)
+    d64, dc, dg = np.zeros((hs.n, 6)), np.zeros((hs.n, 6)), np.zeros((hs.n, 6))
+    g64.propose_with_dats(smc, sites, ppos, masks, d64)
+    g32.propose_with_dats(smc, sites, ppos, masks, dc)
+    assert lib.kmc_set_tuning(g32._handle, 8, 1) == 0
+    g32.propose_with_dats(smc, sites, ppos, masks, dg)
+    assert lib.kmc_set_tuning(g32._handle, 8, 2) != 0
+    act = masks > 0
+    assert not np.array_equal(dc[act], dg[act])
+    assert rel_err(dc[act], dg[act]).max() < 1e-7
+    assert rel_err(dc[act], d64[act]).max() < MIXED_TOL
+    assert rel_err(dg[act], d64[act]).max() < MIXED_TOL
+    g64.free()
+    g32.free()
+
+
 @pytest.mark.parametrize("bc", ["free_space", "pbc"])
 def test_mixed_shared_targets(bc):
     """Many proposals to the same positions (the near field and cell expansion are
