@@ -81,9 +81,24 @@ __device__ __forceinline__ P4 draw(const Key k, const long long step, const uint
 // periodic systems wrap, a free-space lattice masks hops that leave it
 // one thread per (charge, hop): the six nearest-neighbour sites of each charge,
 // the hop's mask (target inside the box, vacant) and the target's centre
-__global__ void k_lat_gen(const int N, const int side, const double spacing, const double half_e, const int wrap,
-                          const int *__restrict__ site_of, const int *__restrict__ occ, double *ppos,
-                          long long *masks, int *tsite)
+// every site's centre (explicit roundings, no contraction, so that host code
+// reproduces the positions bit for bit)
+__global__ void k_site_centres(const int nsites, const int side, const double spacing, const double half_e,
+                               double *centre)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsites) return;
+    const int t[3] = {s % side, (s / side) % side, s / (side * side)};
+    for (int a = 0; a < 3; ++a)
+        centre[3 * (size_t)s + a] =
+            __dadd_rn(__dsub_rn(__dmul_rn((double)t[a], spacing), half_e), __dmul_rn(0.5, spacing));
+}
+
+// hop h of charge i: target site, mask (vacant and inside the box), the site's
+// centre and cell from the tables built at creation
+__global__ void k_lat_gen(const int N, const int side, const int wrap, const int *__restrict__ site_of,
+                          const int *__restrict__ occ, const double *__restrict__ site_centre,
+                          const int *__restrict__ site_cell, double *ppos, long long *masks, int *tsite, int *pcell)
 {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= 6 * N) return;
@@ -102,12 +117,11 @@ __global__ void k_lat_gen(const int N, const int side, const double spacing, con
     const int ts = ok ? t[0] + side * (t[1] + side * t[2]) : s;
     tsite[g] = ts;
     masks[g] = (ok && occ[ts] < 0) ? 1 : 0;
-    const int tx = ts % side, ty = (ts / side) % side, tz = ts / (side * side);
     double *o = ppos + 3 * (size_t)g;
-    // explicit roundings (no contraction) so that host code reproduces the positions bit for bit
-    o[0] = __dadd_rn(__dsub_rn(__dmul_rn((double)tx, spacing), half_e), __dmul_rn(0.5, spacing));
-    o[1] = __dadd_rn(__dsub_rn(__dmul_rn((double)ty, spacing), half_e), __dmul_rn(0.5, spacing));
-    o[2] = __dadd_rn(__dsub_rn(__dmul_rn((double)tz, spacing), half_e), __dmul_rn(0.5, spacing));
+    o[0] = site_centre[3 * (size_t)ts];
+    o[1] = site_centre[3 * (size_t)ts + 1];
+    o[2] = site_centre[3 * (size_t)ts + 2];
+    pcell[g] = site_cell[ts];
 }
 
 // one displacement uniform in [-step, step]^3 per charge, re-drawn while it
@@ -384,6 +398,9 @@ struct kmc_driver {
     double *ppos = nullptr, *diffs = nullptr, *part = nullptr, *rates = nullptr;
     long long *masks = nullptr, *smc = nullptr, *sites = nullptr;
     int *tsite = nullptr, *site_of = nullptr, *occ = nullptr;
+    double *site_centre = nullptr;   // lattice: [nsites][3] site centres
+    int *site_cell = nullptr;        // lattice: the system's cell of each site
+    int *pcell = nullptr;            // lattice: [N * 6] cell of each hop's target
     unsigned int *ticket = nullptr;  // selection blocks finished this step (k_rate_select)
     bool prepared = false;           // proposals of the current state generated and set up
     int64_t seen = -1;               // the system's launch count when they were
@@ -413,13 +430,14 @@ int enqueue_prepare(kmc_driver *d, cudaStream_t st)
     const double half_e = 0.5 * d->E;
     if (d->prm.kind == KMC_DRIVE_LATTICE)
         k_lat_gen<<<(unsigned)((6 * (long long)N + kGenThreads - 1) / kGenThreads), kGenThreads, 0, st>>>(
-            N, d->side, d->spacing, half_e, d->wrap, d->site_of, d->occ, d->ppos, d->masks, d->tsite);
+            N, d->side, d->wrap, d->site_of, d->occ, d->site_centre, d->site_cell, d->ppos, d->masks, d->tsite,
+            d->pcell);
     else
         k_off_gen<<<(unsigned)((N + kGenThreads - 1) / kGenThreads), kGenThreads, 0, st>>>(
             N, half_e, d->prm.step, kmc_int_positions(d->sys), d->key, d->counters, d->ppos);
     if (cudaGetLastError() != cudaSuccess) return KMC_ECUDA;
     return kmc_int_propose_prepare(d->sys, (void *)st, N, d->M, (const int64_t *)d->smc, (const int64_t *)d->sites,
-                                   d->ppos, (const int64_t *)d->masks);
+                                   d->ppos, (const int64_t *)d->masks, d->pcell);
 }
 
 int prepare_branch(void *ctx, void *stream) { return enqueue_prepare((kmc_driver *)ctx, (cudaStream_t)stream); }
@@ -475,8 +493,10 @@ int enqueue_step(kmc_driver *d, cudaStream_t st)
         // plain order: the next step prepares at its start
         return kmc_accept_device(d->sys, (const int64_t *)d->sel_pid, d->sel_pos, d->sel_de);
     }
+    // lattice hops: the next step's set-up reads only the driver's buffers (updated by
+    // the selection) and the charges, so it can start beside k_accept_prep
     if ((rc = kmc_int_accept_device_branch(d->sys, (const int64_t *)d->sel_pid, d->sel_pos, d->sel_de,
-                                           prepare_branch, d)))
+                                           prepare_branch, d, d->prm.kind == KMC_DRIVE_LATTICE)))
         return rc;
     d->prepared = true;
     d->seen = kmc_int_launches(d->sys);
@@ -552,9 +572,18 @@ int kmc_driver_create(kmc_system *s, const kmc_driver_params *p, kmc_driver **ou
                 }
             }
         }
-        if (!own(d, &d->site_of, N) || !own(d, &d->occ, (size_t)nsites) || !own(d, &d->tsite, 6 * (size_t)N)) {
+        if (!own(d, &d->site_of, N) || !own(d, &d->occ, (size_t)nsites) || !own(d, &d->tsite, 6 * (size_t)N) ||
+            !own(d, &d->site_centre, 3 * (size_t)nsites) || !own(d, &d->site_cell, (size_t)nsites) ||
+            !own(d, &d->pcell, 6 * (size_t)N)) {
             release(d);
             return KMC_ENOMEM;
+        }
+        k_site_centres<<<(unsigned)((nsites + 255) / 256), 256, 0, st>>>((int)nsites, d->side, d->spacing, 0.5 * E,
+                                                                         d->site_centre);
+        if (cudaGetLastError() != cudaSuccess ||
+            kmc_int_bin_cells(s, (void *)st, nsites, d->site_centre, d->site_cell) != KMC_OK) {
+            release(d);
+            return KMC_ECUDA;
         }
         if (cudaMemcpyAsync(d->site_of, so.data(), sizeof(int) * N, cudaMemcpyHostToDevice, st) != cudaSuccess ||
             cudaMemcpyAsync(d->occ, occ.data(), sizeof(int) * occ.size(), cudaMemcpyHostToDevice, st) !=

@@ -22,14 +22,21 @@ bool kmc_int_initialised(const kmc_system *s);
 // sort) on a given stream, and the evaluation on the system's stream.  The
 // set-up skips the per-move checks: it serves the device driver, whose moves are
 // valid by construction (spacing / step <= max_move checked at creation,
-// positions inside the box)
+// positions inside the box); prop_cells (optional, [n * max_prop]) gives each
+// proposal's cell as kmc_int_bin_cells computes it
 int kmc_int_propose_prepare(kmc_system *s, void *stream, int64_t n, int64_t max_prop, const int64_t *site_max_counts,
-                            const int64_t *current_sites, const double *prop_positions, const int64_t *prop_masks);
+                            const int64_t *current_sites, const double *prop_positions, const int64_t *prop_masks,
+                            const int *prop_cells);
+// the system's cell of each of n positions (the binning propose applies), on stream
+int kmc_int_bin_cells(kmc_system *s, void *stream, int64_t n, const double *d_pos, int *d_cells);
 int kmc_int_propose_evaluate(kmc_system *s, int64_t n, int64_t max_prop, double *prop_energy_diffs);
-// kmc_accept_device with the caller's work (branch) enqueued on a stream that
-// forks after the store / position update and joins with the accept's end
+// kmc_accept_device with the caller's work (branch) enqueued on a stream that joins
+// with the accept's end and forks after the store / position update, or (early)
+// where the accept is enqueued, for a branch that reads nothing the accept writes
+// (positions, store, expansions, energy)
 int kmc_int_accept_device_branch(kmc_system *s, const int64_t *d_pid, const double *d_new_position,
-                                 const double *d_energy_diff, int (*branch)(void *ctx, void *stream), void *ctx);
+                                 const double *d_energy_diff, int (*branch)(void *ctx, void *stream), void *ctx,
+                                 int early);
 // launches made on the system so far (host count; graph replays add none)
 int64_t kmc_int_launches(const kmc_system *s);
 int kmc_int_tuning(const kmc_system *s, int key);

@@ -221,7 +221,8 @@ int kmc_inject(kmc_system *s, int64_t n, const double *positions, const double *
 #define KMC_TUNE_P2L_FP32_FROM 6 /* double-FP32 accept: orders l >= k in FP32 (0: k = 6; k >= l: none) */
 #define KMC_TUNE_DRIVER_SERIAL 7 /* device driver: 0 next step's set-up beside the accept, 1 plain order */
 #define KMC_TUNE_FSELF_GENERIC 8 /* mixed pbc lattice self term: 0 unrolled L = 12 cubic evaluator, 1 interpreter */
-#define KMC_NTUNE 9
+#define KMC_TUNE_P2L_PAIR 9 /* double-FP32 accept at L = 12, orders from 6 in FP32: 0 column-pair kernel, 1 per-column kernel */
+#define KMC_NTUNE 10
 int kmc_set_tuning(kmc_system *s, int32_t key, int32_t value);
 int kmc_get_tuning(kmc_system *s, int32_t key, int32_t *value_out);
 

@@ -129,11 +129,13 @@ def test_mixed_device_accept_energy_is_fp64():
 @pytest.mark.parametrize("fused", [0, 1])
 @pytest.mark.parametrize("groups", [1, 2, 3])
 @pytest.mark.parametrize("fp32_from", [0, 4, 99])
-def test_mixed_kernel_variants(fused, groups, fp32_from):
+@pytest.mark.parametrize("pair", [0, 1])
+def test_mixed_kernel_variants(fused, groups, fp32_from, pair):
     """Launch-shape and precision variants (fused or split lattice kernels, source
-    groups of the double-FP32 accept, first accept order in FP32: default, 4, none)
-    give the same differences within the mixed tolerance and the same state within
-    1e-12 after accepts."""
+    groups of the double-FP32 accept, first accept order in FP32: default, 4, none;
+    the column-pair or per-column accept kernel at the default split) give the same
+    differences within the mixed tolerance and the same state within 1e-12 after
+    accepts."""
     from coulomb_kmc_gb300 import _native
     hs = LatticeHopSystem(side=16, occupancy=0.25, seed=5)
     (g64, _), (g32, _) = both(hs.positions(), hs.charges(), hs.extent, "pbc", 3, 12, max_move=1.0)
@@ -141,6 +143,7 @@ def test_mixed_kernel_variants(fused, groups, fp32_from):
     assert lib.kmc_set_tuning(g32._handle, 1, fused) == 0
     assert lib.kmc_set_tuning(g32._handle, 0, groups) == 0
     assert lib.kmc_set_tuning(g32._handle, 6, fp32_from) == 0
+    assert lib.kmc_set_tuning(g32._handle, 9, pair) == 0
     rng = np.random.default_rng(3)
     for _ in range(3):
         ppos, masks, tsite = hs.proposals()
