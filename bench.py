@@ -144,13 +144,13 @@ def flop_model(kmc, host_sys, lr_nnz_folded):
 # DRAM traffic per launch of the dominant kernel, from the ncu capture summarised in
 # profiles/fp64_step_lattice48_launch_list.md (dram__bytes_read.sum + dram__bytes_write.sum)
 NCU_TRAFFIC = {"near_far_cell": 12.921088e6}
-# mixed path: profiles/k_near_cell_mixed_lattice48.md, k_p2l_df2_lattice48.md, k_lr_mixed_lattice48.md
-NCU_TRAFFIC_MIXED = {"near_far_cell": 12.667136e6, "accept_p2l": 5.243392e6, "far_lattice": 22.114048e6,
+# mixed path: profiles/k_near_cell_mixed_lattice48.md, k_p2l_pair_lattice48.md, k_lr_mixed_lattice48.md
+NCU_TRAFFIC_MIXED = {"near_far_cell": 12.378624e6, "accept_p2l": 5.167360e6, "far_lattice": 23.233024e6,
                      "far_lattice_old": 1.251584e6}
 # warp instructions per launch from the same ncu capture (smsp__inst_executed.sum), for the
 # issue-slot fraction of the mixed kernels (4 warp instructions per SM per clock)
-NCU_INST_MIXED = {"near_far_cell": 65.003497e6, "accept_p2l": 40.021324e6, "far_lattice": 19.766938e6,
-                  "far_lattice_old": 1.319976e6}
+NCU_INST_MIXED = {"near_far_cell": 40.433271e6, "accept_p2l": 23.066700e6, "far_lattice": 11.877886e6,
+                  "far_lattice_old": 1.332936e6}
 
 
 def issue_fracs(per_launch_ms, clk):

@@ -107,6 +107,8 @@ SIGNATURES = {
     "kmc_driver_sites": ([c_void_p, c_void_p], c_int),
     "kmc_driver_free": ([c_void_p], c_int),
     "kmc_drivers_launch": ([c_void_p, c_int64, c_int64, c_void_p, c_void_p, c_int64], c_int),
+    "kmc_stream_create": ([POINTER(c_void_p)], c_int),
+    "kmc_stream_destroy": ([c_void_p], c_int),
     "kmc_diag_fma_rate": ([c_int32, c_int32, POINTER(c_double)], c_int),
     "kmc_free": ([c_void_p], c_int),
     "kmc_last_error": ([], c_char_p),
@@ -125,6 +127,35 @@ def lib():
             f.restype = rest
         _lib = L
     return _lib
+
+
+class DedicatedStream:
+    """A CUDA stream of its own (kmc_stream_create), usable as a torch stream.
+    torch.cuda.Stream() hands out streams from a fixed pool round-robin, so two of
+    them can be one CUDA stream; a step captured on one while another thread
+    launches on its alias fails.  Drivers and the server use these instead."""
+
+    def __init__(self):
+        import torch
+        h = c_void_p()
+        check(lib().kmc_stream_create(ctypes.byref(h)), "kmc_stream_create")
+        self.handle = h
+        self.stream = torch.cuda.ExternalStream(h.value)
+
+    @property
+    def cuda_stream(self):
+        return self.handle.value
+
+    def close(self):
+        if self.handle is not None and self.handle.value:
+            check(lib().kmc_stream_destroy(self.handle), "kmc_stream_destroy")
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 NKERNELS = 18

@@ -22,6 +22,16 @@
 #include <new>
 #include <vector>
 
+// a failed CUDA call: its name and error string for kmc_last_error, then KMC_ECUDA
+#define DRV_CUDA(call)                                                                                             \
+    do {                                                                                                           \
+        const cudaError_t e_ = (call);                                                                             \
+        if (e_ != cudaSuccess) {                                                                                   \
+            kmc_int_set_error(#call, (int)e_);                                                                     \
+            return KMC_ECUDA;                                                                                      \
+        }                                                                                                          \
+    } while (0)
+
 namespace {
 
 constexpr int kGenThreads = 128;
@@ -435,7 +445,7 @@ int enqueue_prepare(kmc_driver *d, cudaStream_t st)
     else
         k_off_gen<<<(unsigned)((N + kGenThreads - 1) / kGenThreads), kGenThreads, 0, st>>>(
             N, half_e, d->prm.step, kmc_int_positions(d->sys), d->key, d->counters, d->ppos);
-    if (cudaGetLastError() != cudaSuccess) return KMC_ECUDA;
+    DRV_CUDA(cudaGetLastError());
     return kmc_int_propose_prepare(d->sys, (void *)st, N, d->M, (const int64_t *)d->smc, (const int64_t *)d->sites,
                                    d->ppos, (const int64_t *)d->masks, d->pcell);
 }
@@ -487,7 +497,7 @@ int enqueue_step(kmc_driver *d, cudaStream_t st)
     } else {
         k_metropolis<<<1, 32, 0, st>>>(N, d->prm.beta, d->diffs, d->ppos, d->key, o);
     }
-    if (cudaGetLastError() != cudaSuccess) return KMC_ECUDA;
+    DRV_CUDA(cudaGetLastError());
     d->prepared = false;
     if (!pipe) {
         // plain order: the next step prepares at its start
@@ -750,6 +760,23 @@ int kmc_driver_free(kmc_driver *d)
     return KMC_OK;
 }
 
+int kmc_stream_create(void **stream_out)
+{
+    if (!stream_out) return KMC_EINVAL;
+    cudaStream_t st = nullptr;
+    DRV_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    *stream_out = (void *)st;
+    return KMC_OK;
+}
+
+int kmc_stream_destroy(void *stream)
+{
+    if (!stream) return KMC_EINVAL;
+    DRV_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    DRV_CUDA(cudaStreamDestroy((cudaStream_t)stream));
+    return KMC_OK;
+}
+
 int kmc_drivers_launch(kmc_driver **drivers, int64_t n, int64_t steps, void *main_stream, void **worker_streams,
                        int64_t n_workers)
 {
@@ -760,14 +787,14 @@ int kmc_drivers_launch(kmc_driver **drivers, int64_t n, int64_t steps, void *mai
     static std::vector<cudaEvent_t> ev;
     while ((int64_t)ev.size() < n_workers + 1) {
         cudaEvent_t e;
-        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return KMC_ECUDA;
+        DRV_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         ev.push_back(e);
     }
     cudaStream_t ms = (cudaStream_t)main_stream;
-    if (cudaEventRecord(ev[0], ms) != cudaSuccess) return KMC_ECUDA;
+    DRV_CUDA(cudaEventRecord(ev[0], ms));
     const int64_t nw = n_workers < n ? n_workers : n;
     for (int64_t w = 0; w < nw; ++w)
-        if (cudaStreamWaitEvent((cudaStream_t)worker_streams[w], ev[0], 0) != cudaSuccess) return KMC_ECUDA;
+        DRV_CUDA(cudaStreamWaitEvent((cudaStream_t)worker_streams[w], ev[0], 0));
     for (int64_t i = 0; i < n; ++i) {
         const int rc = drivers[i]->graph_pipelined
                            ? ensure_prepared(drivers[i], (cudaStream_t)worker_streams[i % nw])
@@ -776,11 +803,10 @@ int kmc_drivers_launch(kmc_driver **drivers, int64_t n, int64_t steps, void *mai
     }
     for (int64_t k = 0; k < steps; ++k)
         for (int64_t i = 0; i < n; ++i)
-            if (cudaGraphLaunch(drivers[i]->exec, (cudaStream_t)worker_streams[i % nw]) != cudaSuccess)
-                return KMC_ECUDA;
+            DRV_CUDA(cudaGraphLaunch(drivers[i]->exec, (cudaStream_t)worker_streams[i % nw]));
     for (int64_t w = 0; w < nw; ++w) {
-        if (cudaEventRecord(ev[w + 1], (cudaStream_t)worker_streams[w]) != cudaSuccess) return KMC_ECUDA;
-        if (cudaStreamWaitEvent(ms, ev[w + 1], 0) != cudaSuccess) return KMC_ECUDA;
+        DRV_CUDA(cudaEventRecord(ev[w + 1], (cudaStream_t)worker_streams[w]));
+        DRV_CUDA(cudaStreamWaitEvent(ms, ev[w + 1], 0));
     }
     return KMC_OK;
 }

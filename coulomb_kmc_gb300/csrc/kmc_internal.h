@@ -27,6 +27,8 @@ bool kmc_int_initialised(const kmc_system *s);
 int kmc_int_propose_prepare(kmc_system *s, void *stream, int64_t n, int64_t max_prop, const int64_t *site_max_counts,
                             const int64_t *current_sites, const double *prop_positions, const int64_t *prop_masks,
                             const int *prop_cells);
+// records a failed CUDA call for kmc_last_error (the calling thread's message)
+void kmc_int_set_error(const char *what, int cuda_error);
 // the system's cell of each of n positions (the binning propose applies), on stream
 int kmc_int_bin_cells(kmc_system *s, void *stream, int64_t n, const double *d_pos, int *d_cells);
 int kmc_int_propose_evaluate(kmc_system *s, int64_t n, int64_t max_prop, double *prop_energy_diffs);

@@ -51,10 +51,11 @@ class KMCDriver:
                       "kmc_driver_create")
         self.log_capacity = int(log_capacity)
         kmc._energy_valid = False
-        import torch
         # the driver's work runs on its own stream (capturable), ordered after and
-        # before the caller's current stream
-        self.stream = torch.cuda.Stream()
+        # before the caller's current stream; a dedicated stream, not one from
+        # torch's pool (pooled streams alias each other)
+        self._ds = _native.DedicatedStream()
+        self.stream = self._ds.stream
 
     def _enter(self):
         import torch
@@ -63,7 +64,12 @@ class KMCDriver:
 
     def _leave(self):
         import torch
-        torch.cuda.current_stream().wait_stream(self.stream)
+        cur = torch.cuda.current_stream()
+        cur.wait_stream(self.stream)
+        # bind the system back to the caller's stream: the driver's stream is destroyed
+        # with the driver, and the system may outlive it
+        if self.kmc._handle is not None:
+            _native.lib().kmc_set_stream(self.kmc._handle, c_void_p(cur.cuda_stream))
         self.kmc._energy_valid = False
 
     def step(self, n=1):
@@ -127,6 +133,9 @@ class KMCDriver:
         if self._handle is not None and self._handle.value:
             _native.lib().kmc_driver_free(self._handle)
         self._handle = None
+        ds = getattr(self, "_ds", None)
+        if ds is not None:
+            ds.close()
 
     def __del__(self):
         try:

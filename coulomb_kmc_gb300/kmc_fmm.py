@@ -344,6 +344,7 @@ class KMCFMM:
     def free(self):
         """Release the GPU state (kmc_fmm.py:569-577)."""
         if self._handle is not None:
+            self._set_stream()  # the stream last bound (a driver's) may no longer exist
             _native.lib().kmc_free(self._handle)
             self._handle = None
         self._staging = {}

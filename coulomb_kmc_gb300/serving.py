@@ -136,10 +136,13 @@ class Server:
         self.peak_active = 0
         self.budget = float(hbm_budget)
         self.max_active = int(max_active)
-        self.workers = [torch.cuda.Stream() for _ in range(int(n_workers))]
-        self.main = torch.cuda.Stream()
+        # dedicated streams (torch.cuda.Stream() reuses a fixed pool, whose members
+        # would alias the drivers' capture streams)
+        self._owned = [_native.DedicatedStream() for _ in range(int(n_workers) + 1 + max(1, int(n_admit)))]
+        self.workers = [d.stream for d in self._owned[:int(n_workers)]]
+        self.main = self._owned[int(n_workers)].stream
         # admission threads, each building systems on its own stream
-        self.admit_streams = [torch.cuda.Stream() for _ in range(max(1, int(n_admit)))]
+        self.admit_streams = [d.stream for d in self._owned[int(n_workers) + 1:]]
         self.build_s = []
         self.used = 0.0
         self.reserved = 0  # slots taken by systems being built, waiting or running

@@ -275,6 +275,13 @@ int kmc_driver_free(kmc_driver *d);
 int kmc_drivers_launch(kmc_driver **drivers, int64_t n, int64_t steps, void *main_stream, void **worker_streams,
                        int64_t n_workers);
 
+/* A dedicated non-blocking CUDA stream, not taken from any library's stream pool
+ * (pooled streams are handed out round-robin and can alias, which breaks stream
+ * capture on one of them while another thread launches on its alias); destroy
+ * waits for the stream's work.  No reference counterpart. */
+int kmc_stream_create(void **stream_out);
+int kmc_stream_destroy(void *stream);
+
 /* Diagnostic (no reference counterpart): measured FMA throughput of the
  * current device's FP64 (fp64 != 0) or FP32 pipe in TFLOP/s (FMA = 2 flops),
  * the denominator of the roofline fraction of the FMA-bound kernels. */

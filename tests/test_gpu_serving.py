@@ -48,3 +48,27 @@ def test_admission_limits():
     st2 = srv2.serve(rs, realtime=False)
     assert st2["requests"] == len(rs) and srv2.peak_active <= 2
     assert st2["round_ms_p99"] >= st2["round_ms_p50"] > 0.0
+
+
+def test_dedicated_streams_are_distinct():
+    """Drivers and the server run on dedicated streams: torch.cuda.Stream() takes
+    streams from a fixed pool round-robin, so a few dozen of them alias, and a
+    step captured on one stream while another thread launches on its alias fails
+    (cudaErrorStreamCaptureIsolation)."""
+    import torch
+    from coulomb_kmc_gb300 import _native
+    own = [_native.DedicatedStream() for _ in range(48)]
+    assert len({d.cuda_stream for d in own}) == 48
+    assert len({torch.cuda.Stream().cuda_stream for _ in range(48)}) < 48
+    for d in own:
+        d.close()
+
+
+def test_concurrent_admission_many_systems():
+    """Many small systems admitted by several threads while rounds run (the
+    case that aliased pooled streams broke): every request completes."""
+    rs = [Request(rid=i, kind="lattice" if i % 2 else "offlattice", bc="pbc" if i % 2 else "free_space",
+                  n=800 + 37 * i, rounds=3 + i % 4, seed=100 + i, arrival=0.002 * i) for i in range(40)]
+    srv = Server(precision="mixed", n_workers=16, max_active=24, n_admit=4)
+    st = srv.serve(rs, realtime=True)
+    assert st["requests"] == len(rs)
