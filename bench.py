@@ -129,9 +129,13 @@ def flop_model(kmc, host_sys, lr_nnz_folded):
     mpole = 10 * nh + 6 * L        # multipole of one point
     nprop = int(act.sum())
     movers = np.nonzero(masks.sum(axis=1) > 0)[0]
-    near_new = float(np.sum(11 * nb[pcell])) + nprop * (far + 27 * 11 + 4)
+    # the moved pair's self term (27 images) sits in the near-field kernel of the FP64
+    # path and, under pbc, in the per-proposal lattice kernel of the mixed path
+    self_t = 27 * 11 + 4
+    self_in_lr = kmc.precision != "fp64"
+    near_new = float(np.sum(11 * nb[pcell])) + nprop * (far + (0 if self_in_lr else self_t))
     near_old = float(np.sum(11 * nb[st["cells"][movers]])) + len(movers) * (far + 2)
-    lr_new = nprop * (mpole + 4 * nh + lr_nnz_folded + 6)   # a, a.(g-h), a^T U a
+    lr_new = nprop * (mpole + 4 * nh + lr_nnz_folded + 6 + (self_t if self_in_lr else 0))  # a, a.(g-h), a^T U a
     # old side with h = A b kept per charge (mixed path): b and b.g per moving charge;
     # the FP64 path recomputes h every step
     lr_old = len(movers) * (mpole + 4 * nh + (0 if kmc.precision != "fp64" else 2 * 2 * lr_nnz_folded + 4 * nh))
