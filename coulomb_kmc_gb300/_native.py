@@ -14,8 +14,16 @@ _ROOT = os.path.dirname(_PKG)
 BUILD_DIR = os.path.join(_PKG, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libkmc_gb300.so")
 SOURCES = [os.path.join(_PKG, "csrc", "kmc_gb300.cu"), os.path.join(_PKG, "csrc", "kmc_driver.cu")]
-DEPS = SOURCES + [os.path.join(_PKG, "csrc", n) for n in ("kmc_sph.cuh", "kmc_df32.cuh", "kmc_internal.h")] + [
-    os.path.join(_ROOT, "include", "kmc_gb300.h")]
+
+def _deps():
+    """Every source the library is built from: the translation units, every
+    header and fragment in csrc/ and the public header."""
+    csrc = os.path.join(_PKG, "csrc")
+    extra = sorted(os.path.join(csrc, n) for n in os.listdir(csrc) if n.endswith((".cuh", ".h", ".inc")))
+    return SOURCES + extra + [os.path.join(_ROOT, "include", "kmc_gb300.h")]
+
+
+DEPS = _deps()
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 KMC_BC = {"free_space": 0, "27": 1, "pbc": 2}
@@ -85,6 +93,9 @@ SIGNATURES = {
     "kmc_propose_moves_noalloc": ([c_void_p, c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_void_p], c_int),
     "kmc_get_energy": ([c_void_p, POINTER(c_double)], c_int),
     "kmc_get_error": ([c_void_p, POINTER(c_int64), POINTER(c_int64)], c_int),
+    "kmc_store_reserve": ([c_void_p, c_int64], c_int),
+    "kmc_max_occupancy": ([c_void_p, POINTER(c_int64), POINTER(c_int64)], c_int),
+    "kmc_resolve_overflow": ([c_void_p, POINTER(c_int64)], c_int),
     "kmc_read_state": ([c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p], c_int),
     "kmc_info": ([c_void_p, POINTER(c_int64), POINTER(c_int64), POINTER(c_int64)], c_int),
     "kmc_profile": ([c_void_p, c_int32], c_int),

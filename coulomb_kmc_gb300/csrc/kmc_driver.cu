@@ -17,6 +17,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <new>
@@ -420,6 +421,15 @@ struct kmc_driver {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     std::vector<void *> owned;
+    // store headroom: a step moves one charge, so a cell's occupancy grows by at most
+    // one per step; `budget` steps may run before the occupancy is read again (< 0:
+    // the store can never overflow, e.g. a lattice whose cells hold fewer sites than
+    // the store has slots)
+    int64_t budget = 0;
+    int64_t layout = -1;            // the system's buffer layout the captured graph reads
+    cudaEvent_t ev_last = nullptr;  // after the driver's last enqueued step
+    bool ev_recorded = false;
+    cudaStream_t own_stream = nullptr;  // for re-capturing the step after a store growth
 };
 
 namespace {
@@ -517,8 +527,47 @@ void release(kmc_driver *d)
 {
     if (d->exec) cudaGraphExecDestroy(d->exec);
     if (d->graph) cudaGraphDestroy(d->graph);
+    if (d->ev_last) cudaEventDestroy(d->ev_last);
+    if (d->own_stream) cudaStreamDestroy(d->own_stream);
     for (void *p : d->owned) cudaFree(p);
     delete d;
+}
+
+int capture_on(kmc_driver *d, cudaStream_t st);
+
+// Before enqueuing n steps: make sure no cell store can fill during them.  When the
+// budget is spent, wait for the driver's queued steps, read the largest cell
+// occupancy and, if fewer than n free slots remain in some cell, grow the store
+// (the reference grows it when a cell fills, kmc_local.py:318-326; growing earlier
+// changes no result); a captured step reads the store's buffers, so it is captured
+// again after a growth.
+int ensure_headroom(kmc_driver *d, int64_t n)
+{
+    if (d->budget < 0) return KMC_OK;
+    if (d->budget >= n) {
+        d->budget -= n;
+        return KMC_OK;
+    }
+    if (d->ev_recorded) DRV_CUDA(cudaEventSynchronize(d->ev_last));
+    int64_t mx = 0, cap = 0;
+    int rc = kmc_max_occupancy(d->sys, &mx, &cap);
+    if (rc) return rc;
+    if (cap - mx < n) {
+        if ((rc = kmc_store_reserve(d->sys, mx + (n > cap ? n : cap)))) return rc;
+        if ((rc = kmc_max_occupancy(d->sys, &mx, &cap))) return rc;
+    }
+    d->budget = cap - mx - n;
+    if (d->exec && d->layout != kmc_int_layout_gen(d->sys)) return capture_on(d, d->own_stream);
+    return KMC_OK;
+}
+
+// the step enqueued on st (stream-ordered with the driver's previous work): for the
+// headroom check
+int mark_enqueued(kmc_driver *d, cudaStream_t st)
+{
+    DRV_CUDA(cudaEventRecord(d->ev_last, st));
+    d->ev_recorded = true;
+    return KMC_OK;
 }
 
 } // namespace
@@ -595,13 +644,29 @@ int kmc_driver_create(kmc_system *s, const kmc_driver_params *p, kmc_driver **ou
             release(d);
             return KMC_ECUDA;
         }
+        std::vector<int> scell((size_t)nsites);
         if (cudaMemcpyAsync(d->site_of, so.data(), sizeof(int) * N, cudaMemcpyHostToDevice, st) != cudaSuccess ||
             cudaMemcpyAsync(d->occ, occ.data(), sizeof(int) * occ.size(), cudaMemcpyHostToDevice, st) !=
+                cudaSuccess ||
+            cudaMemcpyAsync(scell.data(), d->site_cell, sizeof(int) * scell.size(), cudaMemcpyDeviceToHost, st) !=
                 cudaSuccess ||
             cudaStreamSynchronize(st) != cudaSuccess) {
             release(d);
             return KMC_ECUDA;
         }
+        // a cell never holds more charges than it has sites: with that many slots the
+        // store cannot overflow and no step needs an occupancy check
+        std::vector<int> per((size_t)kmc_int_ncell(s), 0);
+        int most = 0;
+        for (int c : scell) most = std::max(most, ++per[(size_t)c]);
+        int64_t mx = 0, cap = 0;
+        int rc0 = kmc_max_occupancy(s, &mx, &cap);
+        if (!rc0 && cap < most) rc0 = kmc_store_reserve(s, most);
+        if (rc0) {
+            release(d);
+            return rc0;
+        }
+        d->budget = -1;
     } else {
         if (!(p->step > 0.0) || p->step > max_move) {
             delete d;
@@ -643,6 +708,11 @@ int kmc_driver_create(kmc_system *s, const kmc_driver_params *p, kmc_driver **ou
         release(d);
         return rc;
     }
+    if (cudaEventCreateWithFlags(&d->ev_last, cudaEventDisableTiming) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&d->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        release(d);
+        return KMC_ECUDA;
+    }
     *out = d;
     return KMC_OK;
 }
@@ -650,12 +720,12 @@ int kmc_driver_create(kmc_system *s, const kmc_driver_params *p, kmc_driver **ou
 int kmc_driver_step(kmc_driver *d, int64_t nsteps)
 {
     if (!d || nsteps < 0) return KMC_EINVAL;
+    int rc = ensure_headroom(d, nsteps);
+    if (rc) return rc;
     cudaStream_t st = kmc_int_stream(d->sys);
-    for (int64_t k = 0; k < nsteps; ++k) {
-        const int rc = enqueue_step(d, st);
-        if (rc) return rc;
-    }
-    return KMC_OK;
+    for (int64_t k = 0; k < nsteps; ++k)
+        if ((rc = enqueue_step(d, st))) return rc;
+    return nsteps > 0 ? mark_enqueued(d, st) : KMC_OK;
 }
 
 int kmc_driver_capture(kmc_driver *d)
@@ -663,6 +733,12 @@ int kmc_driver_capture(kmc_driver *d)
     if (!d) return KMC_EINVAL;
     cudaStream_t st = kmc_int_stream(d->sys);
     if (!st) return KMC_EINVAL;  // the legacy default stream cannot be captured
+    return capture_on(d, st);
+}
+
+namespace {
+int capture_core(kmc_driver *d, cudaStream_t st)
+{
     if (d->exec) {
         cudaGraphExecDestroy(d->exec);
         d->exec = nullptr;
@@ -686,19 +762,37 @@ int kmc_driver_capture(kmc_driver *d)
     }
     d->graph = g;
     if (cudaGraphInstantiate(&d->exec, g, 0) != cudaSuccess) return KMC_ECUDA;
+    d->layout = kmc_int_layout_gen(d->sys);
     return KMC_OK;
 }
+
+// capture one step on st, with the system bound to st meanwhile (then bound back)
+int capture_on(kmc_driver *d, cudaStream_t st)
+{
+    cudaStream_t prev = kmc_int_stream(d->sys);
+    if (st == prev) return capture_core(d, st);
+    DRV_CUDA(cudaStreamSynchronize(prev));
+    kmc_set_stream(d->sys, (void *)st);
+    const int rc = capture_core(d, st);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    kmc_set_stream(d->sys, (void *)prev);
+    if (rc) return rc;
+    DRV_CUDA(e);
+    return KMC_OK;
+}
+} // namespace
 
 int kmc_driver_launch(kmc_driver *d, int64_t nsteps, void *stream)
 {
     if (!d || nsteps < 0) return KMC_EINVAL;
     if (!d->exec) return KMC_ESTATE;
-    cudaStream_t st = stream ? (cudaStream_t)stream : kmc_int_stream(d->sys);
-    int rc = d->graph_pipelined ? ensure_prepared(d, st) : KMC_OK;
+    int rc = ensure_headroom(d, nsteps);
     if (rc) return rc;
+    cudaStream_t st = stream ? (cudaStream_t)stream : kmc_int_stream(d->sys);
+    if ((rc = d->graph_pipelined ? ensure_prepared(d, st) : KMC_OK)) return rc;
     for (int64_t k = 0; k < nsteps; ++k)
         if (cudaGraphLaunch(d->exec, st) != cudaSuccess) return KMC_ECUDA;
-    return KMC_OK;
+    return nsteps > 0 ? mark_enqueued(d, st) : KMC_OK;
 }
 
 int kmc_driver_counters(kmc_driver *d, int64_t *steps_out, int64_t *accepted_out, int64_t *proposals_out)
@@ -783,6 +877,10 @@ int kmc_drivers_launch(kmc_driver **drivers, int64_t n, int64_t steps, void *mai
     if (!drivers || n < 0 || steps < 0 || !worker_streams || n_workers <= 0) return KMC_EINVAL;
     for (int64_t i = 0; i < n; ++i)
         if (!drivers[i] || !drivers[i]->exec) return KMC_ESTATE;
+    for (int64_t i = 0; i < n; ++i) {
+        const int rc = ensure_headroom(drivers[i], steps);
+        if (rc) return rc;
+    }
     // fork/join events, grown on demand and kept for the process
     static std::vector<cudaEvent_t> ev;
     while ((int64_t)ev.size() < n_workers + 1) {
@@ -804,6 +902,11 @@ int kmc_drivers_launch(kmc_driver **drivers, int64_t n, int64_t steps, void *mai
     for (int64_t k = 0; k < steps; ++k)
         for (int64_t i = 0; i < n; ++i)
             DRV_CUDA(cudaGraphLaunch(drivers[i]->exec, (cudaStream_t)worker_streams[i % nw]));
+    if (steps > 0)
+        for (int64_t i = 0; i < n; ++i) {
+            const int rc = mark_enqueued(drivers[i], (cudaStream_t)worker_streams[i % nw]);
+            if (rc) return rc;
+        }
     for (int64_t w = 0; w < nw; ++w) {
         DRV_CUDA(cudaEventRecord(ev[w + 1], (cudaStream_t)worker_streams[w]));
         DRV_CUDA(cudaStreamWaitEvent(ms, ev[w + 1], 0));

@@ -42,6 +42,10 @@ int kmc_int_accept_device_branch(kmc_system *s, const int64_t *d_pid, const doub
 // launches made on the system so far (host count; graph replays add none)
 int64_t kmc_int_launches(const kmc_system *s);
 int kmc_int_tuning(const kmc_system *s, int key);
+// advances whenever the system's device buffers that a captured step reads are
+// reallocated (store growth): a captured step of an older layout must be captured again
+int64_t kmc_int_layout_gen(const kmc_system *s);
+int kmc_int_ncell(const kmc_system *s);
 bool kmc_int_accept_df32(const kmc_system *s);  // accept contributions in double-FP32 (precision mixed)
 
 } // extern "C"

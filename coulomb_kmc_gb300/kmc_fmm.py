@@ -283,13 +283,19 @@ class KMCFMM:
         else:
             pde[...] = out
 
-    def check_errors(self):
-        """Raise RuntimeError if any proposed move since the last check was invalid."""
+    def error_counts(self):
+        """(invalid proposed moves, store overflows) counted on the device since the last
+        read; reading clears them (synchronises)."""
         bad, ovf = c_int64(), c_int64()
         _native.check(_native.lib().kmc_get_error(self._handle, byref(bad), byref(ovf)), "kmc_get_error")
-        if ovf.value > 0:
+        return bad.value, ovf.value
+
+    def check_errors(self):
+        """Raise RuntimeError if any proposed move since the last check was invalid."""
+        bad, ovf = self.error_counts()
+        if ovf > 0:
             raise RuntimeError("A cell store overflowed during a device-selected accept.")
-        if bad.value > 0:
+        if bad > 0:
             raise RuntimeError("Bad proposed move was detected.")
 
     # ------------------------------------------------------------------
@@ -323,6 +329,32 @@ class KMCFMM:
         _native.check(_native.lib().kmc_accept_device(self._handle, d_pid.data_ptr(), d_new_position.data_ptr(),
                                                       d_energy_diff.data_ptr()), "kmc_accept_device")
         self._energy_valid = False
+
+    def reserve_store(self, capacity):
+        """Set the cell store's capacity (slots per cell) to at least ``capacity`` and the
+        largest occupancy (kmc_store_reserve); returns the new capacity.  Synchronises; a
+        driver captures its step again by itself."""
+        self._assert_init()
+        self._set_stream()
+        _native.check(_native.lib().kmc_store_reserve(self._handle, int(capacity)), "kmc_store_reserve")
+        return self.max_occupancy()[1]
+
+    def max_occupancy(self):
+        """(largest cell occupancy, store capacity); synchronises."""
+        self._assert_init()
+        mx, cap = c_int64(), c_int64()
+        _native.check(_native.lib().kmc_max_occupancy(self._handle, byref(mx), byref(cap)), "kmc_max_occupancy")
+        return mx.value, cap.value
+
+    def resolve_overflow(self):
+        """Apply a device-selected accept that was refused because its new cell was full,
+        after growing the store (kmc_resolve_overflow); True if a move was applied."""
+        self._assert_init()
+        self._set_stream()
+        a = c_int64()
+        _native.check(_native.lib().kmc_resolve_overflow(self._handle, byref(a)), "kmc_resolve_overflow")
+        self._energy_valid = False
+        return bool(a.value)
 
     # ------------------------------------------------------------------
     def state(self):

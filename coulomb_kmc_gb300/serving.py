@@ -149,6 +149,12 @@ class Server:
         self.active = []
         self._cv = threading.Condition()
         self._worker_ptrs = (c_void_p * len(self.workers))(*[s.cuda_stream for s in self.workers])
+        # request id -> "done", "cancelled", "rejected: ..." or "error: ..." (every served request)
+        self.status = {}
+        self._cancel = set()
+        # the round's launch call (kmc_drivers_launch); an attribute so that a test can put a
+        # fake in its place that returns an error code, which ends the run with an error
+        self._launch = _native.lib().kmc_drivers_launch
         # round timing events, created once (before any system captures its step)
         self._e0 = torch.cuda.Event(enable_timing=True)
         self._e1 = torch.cuda.Event(enable_timing=True)
@@ -162,9 +168,8 @@ class Server:
         arr = (c_void_p * len(slots))(*[s.drv._handle.value for s in slots])
         e0, e1 = self._e0, self._e1
         e0.record(self.main)
-        _native.check(_native.lib().kmc_drivers_launch(arr, len(slots), 1, c_void_p(self.main.cuda_stream),
-                                                       self._worker_ptrs, len(self.workers)),
-                      "kmc_drivers_launch")
+        _native.check(self._launch(arr, len(slots), 1, c_void_p(self.main.cuda_stream), self._worker_ptrs,
+                                   len(self.workers)), "kmc_drivers_launch")
         e1.record(self.main)
         e1.synchronize()
         for s in slots:
@@ -178,12 +183,28 @@ class Server:
         nb = estimate_bytes(k.N, req.kind, req.L, k.R)
         return Slot(req=req, kmc=k, drv=d, nbytes=nb, admitted=time.perf_counter())
 
-    def retire(self, slot, free=True):
+    def cancel(self, rid):
+        """Cancel a request (any thread): dropped if not yet admitted, otherwise
+        retired at the next round boundary with status "cancelled"."""
+        with self._cv:
+            self._cancel.add(int(rid))
+
+    def retire(self, slot, free=True, status=None):
+        # the round's work is complete on the main stream: read the system there, not on
+        # the admission stream it was built on (which may be building another system)
+        _native.lib().kmc_set_stream(slot.kmc._handle, c_void_p(self.main.cuda_stream))
         st = slot.drv.stats()
         slot.proposals_per_step = st[2] / max(st[0], 1)
+        if status is None:
+            # the system's device error counters (invalid moves, store overflows): a
+            # kernel-reported error fails the request instead of passing on a wrong state
+            bad, ovf = slot.kmc.error_counts()
+            status = "done" if bad == 0 and ovf == 0 else \
+                "error: device reported %d invalid moves and %d store overflows" % (bad, ovf)
+        self.status[slot.req.rid] = status
         if self.keep_results:
             self.results[slot.req.rid] = {"energy": slot.kmc.energy, "stats": st,
-                                          "positions": slot.kmc.state()["positions"]}
+                                          "positions": slot.kmc.state()["positions"], "status": status}
         if free:
             Server.release(slot)
         return st
@@ -205,6 +226,7 @@ class Server:
         errors = []
 
         graveyard = queue.Queue()
+        closed = queue.Queue()  # (rid, status) of requests that end without running
 
         def bury():
             # memory is released here, off the round loop (freeing may wait for the device)
@@ -227,8 +249,13 @@ class Server:
                 except queue.Empty:
                     continue
                 need = estimate_bytes(r.n, r.kind, r.L, default_r(r.n))
+                with self._cv:
+                    cancelled = r.rid in self._cancel
+                if cancelled:
+                    closed.put((r.rid, "cancelled"))
+                    continue
                 if need > self.budget:
-                    errors.append(MemoryError("request %d needs %.3g bytes, above the budget" % (r.rid, need)))
+                    closed.put((r.rid, "rejected: needs %.3g bytes, above the %.3g byte budget" % (need, self.budget)))
                     continue
                 with self._cv:
                     while not stop.is_set() and (self.used + need > self.budget or self.reserved >= self.max_active):
@@ -258,10 +285,19 @@ class Server:
         round_ms, round_wall, finished = [], [], []
         proposals = 0.0
         busy_t0 = None
+        ended = 0  # requests rejected or cancelled before they ran
+        ok = False
         try:
-            while len(finished) < len(reqs):
+            while len(finished) + ended < len(reqs):
                 if errors:
                     raise errors[0]
+                while True:
+                    try:
+                        rid, why = closed.get_nowait()
+                    except queue.Empty:
+                        break
+                    self.status[rid] = why
+                    ended += 1
                 now = time.perf_counter() - t0
                 while pending and (not realtime or pending[0].arrival <= now):
                     todo.put(pending.pop(0))
@@ -273,6 +309,16 @@ class Server:
                     with self._cv:
                         self.active.append(s)
                         self.peak_active = max(self.peak_active, len(self.active))
+                with self._cv:
+                    cut = [s for s in self.active if s.req.rid in self._cancel]
+                    if cut:
+                        self.active = [s for s in self.active if s.req.rid not in self._cancel]
+                        self.reserved -= len(cut)
+                        self._cv.notify_all()
+                for s in cut:
+                    self.retire(s, free=False, status="cancelled")
+                    ended += 1
+                    graveyard.put(s)
                 if not self.active:
                     time.sleep(0.0005)
                     continue
@@ -294,16 +340,33 @@ class Server:
                         s.finished = time.perf_counter() - t0
                         finished.append(s)
                         graveyard.put(s)
+            ok = True
         finally:
             stop.set()
             for th in threads:
                 th.join(timeout=60)
+            if not ok:
+                # an error ends the run: every system still held is released
+                with self._cv:
+                    held, self.active = self.active, []
+                while True:
+                    try:
+                        held.append(ready.get_nowait())
+                    except queue.Empty:
+                        break
+                for s in held:
+                    try:
+                        self.release(s)
+                    except Exception:
+                        pass
+                    self.used -= s.nbytes
+                self.reserved = 0
             bury()
         wall = time.perf_counter() - (busy_t0 if busy_t0 else t0)
         lat = np.array([s.finished - s.req.arrival for s in finished])
         rm = np.array(round_ms)
         return {
-            "requests": len(finished), "rounds": len(rm), "proposals": proposals,
+            "requests": len(finished), "ended_without_running": ended, "rounds": len(rm), "proposals": proposals,
             "proposals_per_s": proposals / wall if wall > 0 else 0.0, "wall_s": wall,
             "round_ms_p50": float(np.percentile(rm, 50)) if len(rm) else 0.0,
             "round_ms_p99": float(np.percentile(rm, 99)) if len(rm) else 0.0,

@@ -124,21 +124,29 @@ int kmc_accept(kmc_system *s, int64_t pid, const double new_position[3]);
 int kmc_accept_device(kmc_system *s, const int64_t *d_pid, const double *d_new_position,
                       const double *d_energy_diff);
 
-/* Allocation-free variant of kmc_propose_moves, for callers that must not
- * allocate device memory during the call (for example code that runs while
- * another component owns the allocator, or that is invoked from inside a
- * stream capture region).  It has no counterpart in the reference.
+/* Allocation-free variant of kmc_propose_moves.  It has no counterpart in the
+ * reference.  It serves callers that cannot allocate device memory when they
+ * need energy differences: an application whose own memory pool has already
+ * claimed the device memory it may use (a cudaMalloc from this library would
+ * fail or fragment that pool), or a loop that cannot afford the device
+ * synchronisation a cudaFree implies.
  * All pointers are device memory: particle ids d_pids[nump],
  * d_exclusive_sum[nump+1] (proposal offsets), d_new_positions[total][3];
  * d_diffs[total] receives dE * energy_unit, in proposal order.  FP64.
- * Scratch is a fixed file-scope device array, not the handle's buffers:
- * limits 4096 moving charges and 16384 proposals per call (larger calls
- * return KMC_EINVAL with a message).  The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress) with that device current;
- * make that first call before any stream capture.  Every call on a device
- * shares the array, so calls that overlap on the GPU (different streams or
- * handles) race; serialise them.  Nothing in it needs clearing: each call
- * writes every element it reads.  Does not synchronise. */
+ * Scratch is a fixed file-scope device array of about 41 KB that every device
+ * which loads the library holds until exit, not the handle's buffers: limits
+ * 4096 moving charges and 16384 proposals per call (larger calls return
+ * KMC_EINVAL with a message).  Set-up: the first call on a device (and the
+ * first after that device's context was replaced) looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  Every call on a device shares the array and it
+ * keeps the last call's contents, so calls that overlap on the GPU (different
+ * streams or handles) race; serialise them.  Each call writes every element of
+ * it that the call reads.  Inputs are checked on the device before use: ids
+ * outside [0, N) or offsets that do not start at 0, decrease or end at another
+ * total than `total` make every output NaN; a proposed position outside the box,
+ * not finite or beyond max_move makes its output NaN; both are counted as bad
+ * moves (kmc_get_error).  Does not synchronise. */
 int kmc_propose_moves_noalloc(kmc_system *s, int64_t nump, int64_t total, const int64_t *d_pids,
                               const int64_t *d_exclusive_sum, const double *d_new_positions, double *d_diffs);
 
@@ -148,6 +156,24 @@ int kmc_get_energy(kmc_system *s, double *energy_out);
 /* Read and clear the device error counters (synchronises):
  * bad_moves = invalid proposals since the last call, overflow = store overflows. */
 int kmc_get_error(kmc_system *s, int64_t *bad_moves, int64_t *overflow);
+
+/* Cell store capacity.  The reference grows a cell's particle store when an
+ * accepted move fills it (LocalParticleData, kmc_local.py:318-326, 558-580);
+ * kmc_accept does the same on the host before it launches.  A device-selected
+ * accept (kmc_accept_device, the device driver) cannot reallocate: when its new
+ * cell is full it leaves the whole state untouched, counts an overflow
+ * (kmc_get_error) and keeps the move; every later device-selected accept is
+ * refused the same way until kmc_resolve_overflow grows the store and applies
+ * the kept move (*applied_out = 1; 0 when nothing was kept).  kmc_accept returns
+ * KMC_EOVERFLOW while a move is kept.  The device driver avoids the case: it
+ * reads the occupancy before a cell could fill and grows the store first.
+ * kmc_store_reserve sets the capacity (slots per cell, rounded up to a multiple
+ * of 4) to at least `capacity` and at least the largest occupancy; it may also
+ * shrink the store.  Synchronises; captured steps must be captured again after it.
+ * kmc_max_occupancy: the largest cell occupancy and the capacity (synchronises). */
+int kmc_store_reserve(kmc_system *s, int64_t capacity);
+int kmc_max_occupancy(kmc_system *s, int64_t *max_out, int64_t *capacity_out);
+int kmc_resolve_overflow(kmc_system *s, int64_t *applied_out);
 
 /* Copy state to host for inspection (synchronises; any pointer may be NULL):
  * positions[n][3], cells[n] (linear finest-level cell, x fastest),
@@ -222,7 +248,9 @@ int kmc_inject(kmc_system *s, int64_t n, const double *positions, const double *
 #define KMC_TUNE_DRIVER_SERIAL 7 /* device driver: 0 next step's set-up beside the accept, 1 plain order */
 #define KMC_TUNE_FSELF_GENERIC 8 /* mixed pbc lattice self term: 0 unrolled L = 12 cubic evaluator, 1 interpreter */
 #define KMC_TUNE_P2L_PAIR 9 /* double-FP32 accept at L = 12, orders from 6 in FP32: 0 column-pair kernel, 1 per-column kernel */
-#define KMC_NTUNE 10
+#define KMC_TUNE_P2L64 10 /* FP64 accept at L = 8, 12, 16: 0 column-pair kernel, 1 per-column kernel */
+#define KMC_TUNE_P2L64_GROUPS 11 /* FP64 column-pair accept: k source-group pairs, 2k groups (1..4; 0: 4 groups) */
+#define KMC_NTUNE 12
 int kmc_set_tuning(kmc_system *s, int32_t key, int32_t value);
 int kmc_get_tuning(kmc_system *s, int32_t key, int32_t *value_out);
 
