@@ -1,38 +1,44 @@
-"""Benchmark: proposal energy differences per second on the pbc lattice-hop workload.
+"""Benchmark: proposal energy differences per second, batched mixed precision against
+plain FP64 (the metric's own configuration).
 
-Workload (one system per GPU): simple-cubic lattice of 48^3 sites (spacing 1,
-box edge 48, periodic), 27,648 charges (25 % occupancy, +-1 balanced, seed 1),
-FMM depth R=5 (16^3 cells), L=12.  One step = one rejection-free KMC step:
-every charge proposes a hop to each vacant nearest-neighbour site (~124k
-proposals), all proposal energy differences are computed, one move is chosen
-with rate exp(-beta dE / 2), beta = 2, and accepted.
+Default workload (--workload batched): 256 independent off-lattice KMC systems, N
+log-uniform in [2,000, 131,072] (seed 3), half free space and half pbc, 0.25 charges
+per unit volume, R = max(2, ceil(log8(N/8))), L = 12.  One step = one round: every
+system advances one KMC step -- every charge proposes a displacement uniform in
+[-0.5, 0.5]^3, all differences are computed, one random charge's proposal is accepted
+by Metropolis at beta = 1 -- all systems' captured step graphs launched together.
+Precision: the mixed mode with FP64 accept contributions (near field and harmonic
+evaluation in FP32 / double-FP32; accept increments, the lattice operator, the energy
+and the final difference in FP64).
 
-Timed arms:
-  value : device resident -- the library's device-side KMC driver (proposal
-          generation, rejection-free selection and occupancy kernels) around its
-          propose and accept kernels, one captured CUDA graph per step; L2 flushed
-          (256 MiB write) between timed steps.
-  e2e   : the reference-facing API with host (numpy) buffers, exactly as the
-          reference's driver uses it: host bookkeeping, propose_with_dats with
-          host<->device copies, host selection, accept.
-  --impl reference : the reference's CPU path as restated by the oracle
-          (ppmd/coulomb_kmc cannot be built here), all host threads.
+Timed arms and keys:
+  value  : device resident rounds (CUDA events per round on the server's main stream);
+           the systems' state (~1 GB) is far above the 129 MB L2.
+  e2e    : the reference-facing API with host (numpy) buffers, exactly as the
+           reference's driver uses it: host proposals, propose_with_dats with host <->
+           device copies, host Metropolis, accept -- every system every round.
+  fp64   : the same systems on the plain FP64 path; mixed_vs_fp64 the ratio.
+  mixed_error : mixed vs FP64 differences and Metropolis decisions on sampled systems.
+  config1 / config2 : free space N=1,000 (R=3, L=12, Metropolis, 100 steps) and the
+           48^3 pbc lattice-hop workload (27,648 charges, R=5, L=12, rejection-free).
+  cpu_baseline / --impl reference : the reference's CPU path as restated by the oracle
+           (ppmd/coulomb_kmc cannot be built here), all host threads, on a bounded sample.
 
 Other workloads (--workload; each prints its own JSON line):
+  lattice48       : the 48^3 lattice-hop workload as the headline line.
   precision_split : 64^3 lattice, 65,536 charges, R=6, L in {8, 12, 16}: mixed vs
                     FP64 error (max / RMS relative dE, Metropolis agreement) and
                     throughput of both paths.
-  batched         : independent off-lattice systems (N log-uniform in
-                    [2,000, 131,072], half free_space, half pbc, density 0.25,
-                    L=12), one step of every system per round through one
-                    multi-stream launch of their captured step graphs; mixed vs FP64.
+  batched_streams : the batched workload through per-system graph launches on a pool
+                    of worker streams, --systems/--rounds, mixed (double-FP32 accept)
+                    vs FP64.
   serving         : Poisson request stream through the continuous-batching
                     server, p50/p99 round latency and throughput, against FP64
                     one system at a time.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload ...]
-Multi-GPU (torchrun): independent replicas, one system per rank, no collective
-on the data path; value = proposals over all ranks / max rank time.
+Multi-GPU (torchrun): independent replicas, no collective on the data path; value =
+proposals over all ranks / max rank time.
 """
 import argparse
 import json
@@ -145,16 +151,17 @@ def flop_model(kmc, host_sys, lr_nnz_folded):
             "accept_p2l": p2l, "proposals": nprop, "mean_neighbours": float(np.mean(nb[pcell]))}
 
 
-# DRAM traffic per launch of the dominant kernel, from the ncu capture summarised in
-# profiles/fp64_step_lattice48_launch_list.md (dram__bytes_read.sum + dram__bytes_write.sum)
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the lattice
+# workload's kernels from an earlier ncu capture of the same kernels: not measured by this
+# program, and stale once a kernel changes; the line says so beside the figure.
 NCU_TRAFFIC = {"near_far_cell": 12.921088e6}
-# mixed path: profiles/k_near_cell_mixed_lattice48.md, k_p2l_pair_lattice48.md, k_lr_mixed_lattice48.md
 NCU_TRAFFIC_MIXED = {"near_far_cell": 12.378624e6, "accept_p2l": 5.167360e6, "far_lattice": 23.233024e6,
                      "far_lattice_old": 1.251584e6}
-# warp instructions per launch from the same ncu capture (smsp__inst_executed.sum), for the
-# issue-slot fraction of the mixed kernels (4 warp instructions per SM per clock)
+# warp instructions per launch (smsp__inst_executed.sum) from the same earlier capture, for
+# the issue-slot fraction of the mixed kernels (4 warp instructions per SM per clock)
 NCU_INST_MIXED = {"near_far_cell": 40.433271e6, "accept_p2l": 23.066700e6, "far_lattice": 11.877886e6,
                   "far_lattice_old": 1.332936e6}
+NCU_SOURCE = "earlier ncu capture of the same kernels on this workload, not measured in this run"
 
 
 def issue_fracs(per_launch_ms, clk):
@@ -241,13 +248,13 @@ def run_reference(args):
         return
     cores = os.cpu_count()
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-    steps = max(1, min(args.steps, args.ref_steps))
-    v, dt, nprop = cpu_reference(steps, min(args.warmup, 1), SIDE)
+    steps = max(1, args.steps)
+    v, dt, nprop = cpu_reference(steps, args.warmup, SIDE)
     sample = (f"{steps} KMC steps of the {SIDE}^3 lattice-hop workload ({nprop} proposals), oracle restatement "
               f"of the reference's generated C (ppmd is unavailable), OpenMP {cores} threads; "
               f"initial expansions zero (the operation count does not depend on their values)")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
-            "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": workload_config(SIDE, "fp64"),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
@@ -315,7 +322,7 @@ def timed_loop(kmc, drv, steps, warmup, flush, sampler=None, graph=True):
     return per_step, nprop, per_step_launches * steps, clk
 
 
-def mixed_error_stats(side, local, nsteps=3, seed=11):
+def mixed_error_stats(side, local, nsteps=3, seed=11, precision="mixed"):
     """Mixed vs FP64 on identical states: relative dE error (denominator max(|dE|,1))
     and Metropolis-decision agreement (u < exp(-beta dE) with shared u)."""
     from coulomb_kmc_gb300 import KMCFMM
@@ -323,10 +330,10 @@ def mixed_error_stats(side, local, nsteps=3, seed=11):
     from coulomb_kmc_gb300.workloads import LatticeHopSystem
     hs = LatticeHopSystem(side, OCC, seed=seed)
     ks = {}
-    for prec in ("fp64", "mixed"):
+    for name, prec in (("fp64", "fp64"), ("mixed", precision)):
         st = make_state(hs.positions(), hs.charges(), hs.extent)
-        ks[prec] = KMCFMM(st.P, st.Q, st.domain, r=R, l=L, boundary_condition="pbc", max_move=1.0, precision=prec)
-        ks[prec].initialise()
+        ks[name] = KMCFMM(st.P, st.Q, st.domain, r=R, l=L, boundary_condition="pbc", max_move=1.0, precision=prec)
+        ks[name].initialise()
     rng = np.random.default_rng(5)
     errs, agree, total, sel_agree = [], 0, 0, 0
     for _ in range(nsteps):
@@ -542,26 +549,507 @@ def bench_serving(args):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------------------
+# Batched replicas (the metric's own configuration): 256 independent off-lattice
+# systems, N log-uniform in [2,000, 131,072] (seed 3), half free space and half
+# pbc, density 0.25, R = max(2, ceil(log8(N/8))), L = 12; one proposal per charge
+# per round (uniform displacement in [-0.5, 0.5]^3, re-drawn inside the box) and a
+# Metropolis accept (beta = 1) of one random charge's proposal, every system every
+# round.
+# ---------------------------------------------------------------------------
+C4_BETA, C4_STEP = 1.0, 0.5
+
+
+def config4_requests(n_systems, seed=3):
+    from coulomb_kmc_gb300.serving import Request
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(n_systems):
+        n = int(round(np.exp(rng.uniform(np.log(2000), np.log(131072)))))
+        bc = "free_space" if i % 2 == 0 else "pbc"
+        reqs.append(Request(rid=i, kind="offlattice", bc=bc, n=n, rounds=0, seed=int(rng.integers(1, 2 ** 31)),
+                            L=12, beta=C4_BETA))
+    return reqs
+
+
+def config4_workload(n_systems):
+    return (f"{n_systems} independent off-lattice systems, N log-uniform in [2000, 131072] (seed 3), half "
+            f"free_space / half pbc, density 0.25, R=max(2, ceil(log8(N/8))), L=12, one proposal per charge per "
+            f"round (uniform in [-0.5, 0.5]^3), Metropolis beta=1 on one random charge per system per round")
+
+
+def build_kmcs(reqs, precision, threads=4):
+    """Create and initialise every system (no driver yet), on `threads` host threads,
+    each with its own CUDA stream.  Returns [(KMCFMM, extent)] in request order."""
+    import torch
+    from concurrent.futures import ThreadPoolExecutor
+    from coulomb_kmc_gb300 import KMCFMM, _native
+    from coulomb_kmc_gb300.dats import make_state
+    from coulomb_kmc_gb300.serving import default_r, system_inputs
+    streams = [_native.DedicatedStream() for _ in range(threads)]
+    dev = torch.cuda.current_device()
+
+    def one(i):
+        r = reqs[i]
+        torch.cuda.set_device(dev)
+        st_ = streams[i % threads]
+        with torch.cuda.stream(st_.stream):
+            pos, q, E, _, _ = system_inputs(r)
+            st = make_state(pos, q, E)
+            k = KMCFMM(st.P, st.Q, st.domain, r=default_r(len(q)), l=r.L, boundary_condition=r.bc,
+                       max_move=C4_STEP, precision=precision)
+            k.initialise()
+            st_.stream.synchronize()
+        return k, E
+
+    with ThreadPoolExecutor(threads) as ex:
+        out = list(ex.map(one, range(len(reqs))))
+    torch.cuda.synchronize()
+    for k, _ in out:
+        k._set_stream()  # off the build streams, which end here
+    for st_ in streams:
+        st_.close()
+    return out
+
+
+def offlattice_proposals(pos, E, rng):
+    h = 0.5 * E
+    prop = pos + rng.uniform(-C4_STEP, C4_STEP, size=pos.shape)
+    bad = np.any(np.abs(prop) > h, axis=1)
+    while np.any(bad):
+        prop[bad] = pos[bad] + rng.uniform(-C4_STEP, C4_STEP, size=(int(bad.sum()), 3))
+        bad = np.any(np.abs(prop) > h, axis=1)
+    return prop
+
+
+class HostRound:
+    """One Metropolis round of every system through the reference-facing API with host
+    (numpy) buffers: proposals generated on the host, propose_with_dats (host -> device
+    copies of the proposals, device -> host copy of the differences), Metropolis on the
+    host, accept.  Buffers per system are allocated once."""
+
+    def __init__(self, kmcs, seed=7):
+        self.kmcs = kmcs
+        self.rng = np.random.default_rng(seed)
+        self.buf = []
+        for k, E in kmcs:
+            n = k.N
+            self.buf.append((np.array([1], np.int64), np.zeros((n, 1), np.int64), np.ones((n, 1), np.int64),
+                             np.zeros((n, 1))))
+        self.proposals = 0
+        self.h2d = 0
+        self.d2h = 0
+
+    def run(self, kmc_list=None):
+        for (k, E), (smc, sites, masks, diffs) in zip(self.kmcs, self.buf):
+            pos = k.positions if isinstance(k.positions, np.ndarray) else np.asarray(k._positions_host())
+            prop = offlattice_proposals(np.asarray(pos, dtype=np.float64).reshape(-1, 3), E, self.rng)
+            k.propose_with_dats(smc, sites, prop, masks, diffs)
+            pid = int(self.rng.integers(0, k.N))
+            if self.rng.uniform() < np.exp(-C4_BETA * diffs[pid, 0]):
+                k.accept((pid, prop[pid].copy()))
+            self.proposals += k.N
+            self.h2d += smc.nbytes + sites.nbytes + prop.nbytes + masks.nbytes + diffs.nbytes
+            self.d2h += diffs.nbytes + 16
+
+
+def make_slots(reqs, kmcs):
+    from coulomb_kmc_gb300.driver import KMCDriver
+    from coulomb_kmc_gb300.serving import Slot
+    slots = []
+    for r, (k, E) in zip(reqs, kmcs):
+        d = KMCDriver(k, "offlattice", C4_BETA, seed=r.seed, step=C4_STEP)
+        d.capture()
+        slots.append(Slot(req=r, kmc=k, drv=d, nbytes=0, admitted=0.0))
+    import torch
+    torch.cuda.synchronize()
+    return slots
+
+
+def timed_rounds(srv, slots, steps, warmup, sampler=None):
+    """W untimed rounds, then exactly `steps` rounds, each timed with CUDA events on the
+    server's main stream (every system one KMC step per round)."""
+    import torch
+    for _ in range(warmup):
+        srv.round(slots)
+    torch.cuda.synchronize()
+    p0 = sum(sl.drv.stats()[2] for sl in slots)
+    if sampler:
+        sampler.start()
+    torch.cuda.synchronize()
+    ms = np.array([srv.round(slots) for _ in range(steps)])
+    torch.cuda.synchronize()
+    clk = sampler.stop() if sampler else None
+    p1 = sum(sl.drv.stats()[2] for sl in slots)
+    return ms, p1 - p0, clk
+
+
+def free_slots(slots):
+    for sl in slots:
+        sl.drv.free()
+        sl.kmc.free()
+
+
+def config4_error_stats(reqs, nsys=6, rounds=2, seed=11):
+    """Mixed (FP64 accept) vs plain FP64 on identical states for a sample of the
+    systems (smallest and largest of each boundary condition, two in between): relative
+    difference error (denominator max(|dE|, 1)) and Metropolis-decision agreement with
+    shared uniforms; both take the FP64 decision so the states stay identical."""
+    idx = sorted(range(len(reqs)), key=lambda i: reqs[i].n)
+    fs = [i for i in idx if reqs[i].bc == "free_space"]
+    pb = [i for i in idx if reqs[i].bc == "pbc"]
+    pick = sorted(set([fs[0], fs[-1], pb[0], pb[-1], fs[len(fs) // 2], pb[len(pb) // 2]]))[:nsys]
+    sub = [reqs[i] for i in pick]
+    mx = build_kmcs(sub, "mixed_fp64_accept", threads=2)
+    f64 = build_kmcs(sub, "fp64", threads=2)
+    rng = np.random.default_rng(seed)
+    errs, agree, total = [], 0, 0
+    per = {}
+    for (km, E), (kf, _), r in zip(mx, f64, sub):
+        e_sys = []
+        for _ in range(rounds):
+            pos = np.asarray(kf._positions_host(), dtype=np.float64).reshape(-1, 3)
+            prop = offlattice_proposals(pos, E, rng)
+            n = kf.N
+            d = {}
+            for name, k in (("m", km), ("f", kf)):
+                d[name] = np.zeros((n, 1))
+                k.propose_with_dats(np.array([1], np.int64), np.zeros((n, 1), np.int64), prop,
+                                    np.ones((n, 1), np.int64), d[name])
+            e = np.abs(d["m"] - d["f"]) / np.maximum(np.abs(d["f"]), 1.0)
+            e_sys.append(e.ravel())
+            u = rng.uniform(size=n)
+            agree += int(np.sum((u < np.exp(-C4_BETA * d["m"][:, 0])) == (u < np.exp(-C4_BETA * d["f"][:, 0]))))
+            total += n
+            pid = int(rng.integers(0, n))
+            if u[pid] < np.exp(-C4_BETA * d["f"][pid, 0]):
+                for k in (km, kf):
+                    k.accept((pid, prop[pid].copy()))
+        es = np.concatenate(e_sys)
+        errs.append(es)
+        per[f"{r.bc} N={r.n}"] = {"max_rel": float(es.max()), "rms_rel": float(np.sqrt(np.mean(es * es)))}
+        km.free()
+        kf.free()
+    e = np.concatenate(errs)
+    return {"max_rel": float(e.max()), "rms_rel": float(np.sqrt(np.mean(e * e))), "proposals": int(e.size),
+            "metropolis_decision_agreement": agree / total, "tolerance": 1e-6, "per_system": per,
+            "sample": f"{len(sub)} systems x {rounds} rounds (smallest, middle and largest of each boundary condition)"}
+
+
+def launches_per_step(slots):
+    """Kernel launches of one step of each system (the library's own launch counter over
+    one eager step, plus the driver's generation and selection kernels)."""
+    import torch
+    total = 0
+    for sl in slots:
+        kernel_times(sl.kmc)  # reads and resets the handle's launch counter
+        sl.drv.step(1)
+        torch.cuda.synchronize()
+        _, l1 = kernel_times(sl.kmc)
+        total += l1 + DRIVER_KERNELS_PER_STEP
+    return total
+
+
+def offlattice_flop_model(kmc, L_):
+    """Algorithmic flops of one launch of the mixed near-field kernel (near_far_cell) on an
+    off-lattice system: every charge's proposal (new side) and old position (old side)
+    against its 27 neighbour cells, plus the cell-expansion evaluation (survey counting
+    convention: add/mul 1, FMA 2, rsqrt 1)."""
+    st = kmc.state()
+    n = round(len(st["occupancy"]) ** (1 / 3))
+    occ = st["occupancy"].reshape(n, n, n)
+    nb = np.zeros_like(occ)
+    from coulomb_kmc_gb300.common import BCType
+    per = kmc.boundary_condition != BCType.FREE_SPACE
+    for dz in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dx in (-1, 0, 1):
+                sh = np.roll(occ, shift=(dz, dy, dx), axis=(0, 1, 2))
+                if not per:
+                    if dz:
+                        sh[0 if dz > 0 else -1, :, :] = 0
+                    if dy:
+                        sh[:, 0 if dy > 0 else -1, :] = 0
+                    if dx:
+                        sh[:, :, 0 if dx > 0 else -1] = 0
+                nb += sh
+    nb = nb.reshape(-1)
+    nh = L_ * (L_ + 1) // 2
+    far = 12 * nh + 6 * L_
+    cells = st["cells"]
+    # a proposal lands in its own cell or a neighbour: the old cell's neighbour count
+    # stands for both sides (displacements are at most 0.5 of a ~5-wide cell)
+    pair = float(np.sum(11 * nb[cells]))
+    return 2 * pair + 2 * len(cells) * far, float(np.mean(nb[cells]))
+
+
+def bench_config4(args, rank, world, local):
+    """The headline: batched replicas of the metric's configuration (see config4_requests)."""
+    import torch
+    from coulomb_kmc_gb300 import _native
+    from coulomb_kmc_gb300.serving import Server
+    reqs = config4_requests(args.systems)
+    prec = args.precision
+    t0 = time.perf_counter()
+    kmcs = build_kmcs(reqs, prec, threads=args.build_threads)
+    build_s = time.perf_counter() - t0
+    extras = {}
+    # e2e: the reference-facing API with host buffers (before the device drivers exist)
+    if not args.no_extras:
+        hr = HostRound(kmcs)
+        hr.run()
+        torch.cuda.synchronize()
+        p0, b0, c0 = hr.proposals, hr.h2d, hr.d2h
+        t1 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            hr.run()
+        torch.cuda.synchronize()
+        e2e_dt = time.perf_counter() - t1
+        nr = max(args.e2e_steps, 1)
+        extras["e2e"] = {"value": (hr.proposals - p0) / e2e_dt, "unit": UNIT,
+                         "h2d_bytes_per_step": int((hr.h2d - b0) / nr), "d2h_bytes_per_step": int((hr.d2h - c0) / nr),
+                         "steps": args.e2e_steps,
+                         "path": "KMCFMM.propose_with_dats with numpy buffers (pinned staging, H2D of every "
+                                 "proposal array, D2H of the differences) + host Metropolis + KMCFMM.accept, "
+                                 "every system every round"}
+    slots = make_slots(reqs, kmcs)
+    launches = launches_per_step(slots) if not args.no_extras else None
+    srv = Server(precision=prec, n_workers=args.workers)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    ms, nprop, clk = timed_rounds(srv, slots, args.steps, args.warmup, ClockSampler(local))
+    t_ms = float(ms.sum())
+    value = nprop / (t_ms * 1e-3)
+    print(json.dumps({"stage": "timed rounds", "value": value, "round_ms_p50": float(np.percentile(ms, 50)),
+                      "round_ms_p99": float(np.percentile(ms, 99)), "build_s": build_s,
+                      "e2e": extras.get("e2e", {}).get("value")}), file=sys.stderr, flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        tot = torch.tensor([t_ms, float(nprop)], dtype=torch.float64, device="cuda")
+        tmax = tot[0:1].clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        dist.all_reduce(tot[1:2], op=dist.ReduceOp.SUM)
+        t_ms, nprop = float(tmax[0]), float(tot[1])
+        value = nprop / (t_ms * 1e-3)
+    if not args.no_extras:
+        # per-kernel times of the largest system of each boundary condition (separate pass)
+        big = {}
+        for bc in ("pbc", "free_space"):
+            i = max((j for j in range(len(reqs)) if reqs[j].bc == bc), key=lambda j: reqs[j].n)
+            sl = slots[i]
+            _native.lib().kmc_profile(sl.kmc._handle, 1)
+            kernel_times(sl.kmc)
+            sl.drv.step(5)
+            torch.cuda.synchronize()
+            kt, _ = kernel_times(sl.kmc)
+            _native.lib().kmc_profile(sl.kmc._handle, 0)
+            per_launch = {k: v[0] / max(v[1], 1) for k, v in kt.items() if v[1] > 0}
+            fl, mnb = offlattice_flop_model(sl.kmc, 12)
+            big[bc] = {"n": reqs[i].n, "per_kernel_ms": {k: round(v, 5) for k, v in per_launch.items()},
+                       "near_flops": fl, "mean_neighbours": mnb}
+        free_slots(slots)
+        peak64, peak32 = fma_peak(True), fma_peak(False)
+        b = big["pbc"]
+        nf_ms = b["per_kernel_ms"].get("near_far_cell")
+        ach = b["near_flops"] / (nf_ms * 1e-3) / 1e12 if nf_ms else None
+        extras["roofline"] = {
+            "bound": "fp32", "kernel": "near_far_cell", "achieved": ach, "peak": peak32, "unit": "TFLOP/s",
+            "frac": ach / peak32 if ach else None, "traffic": None,
+            "kernel_workload": f"largest pbc system (N={b['n']}), 5 steps, CUDA events per launch",
+            "peak_source": "measured in this run with kmc_diag_fma_rate (FMA issue rate of the FP32 pipe); "
+                           "MEASURED_PEAKS.json holds HBM and bf16 only, and the kernel is arithmetic bound",
+            "peaks_measured": {"fp64_tflops": peak64, "fp32_tflops": peak32},
+            "flops_convention": "algorithmic flops of the FP64 algorithm (add/mul 1, FMA 2, rsqrt 1); the mixed "
+                                "kernel spends several FP32 instructions per algorithmic flop",
+            "flops_per_launch": b["near_flops"], "mean_neighbours_per_proposal": b["mean_neighbours"],
+            "per_kernel_ms_largest": {k: v["per_kernel_ms"] for k, v in big.items()},
+            "traffic_note": "not captured in this run; the ncu captures summarised with the profiles give the "
+                            "DRAM bytes per launch"}
+        # the plain FP64 path on the same systems
+        k64 = build_kmcs(reqs, "fp64", threads=args.build_threads)
+        s64 = make_slots(reqs, k64)
+        srv64 = Server(precision="fp64", n_workers=args.workers)
+        ms64, np64, _ = timed_rounds(srv64, s64, max(2, args.fp64_rounds), 1)
+        free_slots(s64)
+        extras["fp64"] = {"value": np64 / (ms64.sum() * 1e-3), "round_ms_p50": float(np.percentile(ms64, 50)),
+                          "round_ms_p99": float(np.percentile(ms64, 99)), "rounds": len(ms64)}
+        extras["mixed_vs_fp64"] = value / extras["fp64"]["value"]
+        print(json.dumps({"stage": "fp64", **extras["fp64"]}), file=sys.stderr, flush=True)
+        extras["mixed_error"] = config4_error_stats(reqs)
+        if rank == 0:
+            cores = os.cpu_count()
+            v, dt, npc, smp = cpu_config4(reqs, args.cpu_rounds, 1)
+            extras["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": smp}
+        extras["config1"] = bench_config1(args)
+        extras["config2"] = bench_config2_extra(args, rank, local)
+    else:
+        free_slots(slots)
+    return value, t_ms, nprop, ms, clk, launches, build_s, extras
+
+
+def cpu_config4(reqs, rounds, warmup, sample=None):
+    """The reference's CPU path (oracle restatement, OpenMP on all host cores) on a
+    bounded sample of the batched workload: `rounds` Metropolis rounds of each sampled
+    system (one proposal per charge, one accept).  Initial expansions zero: the
+    operation count does not depend on their values."""
+    from oracle import kmc_oracle as ko
+    from coulomb_kmc_gb300.lattice import lattice_operator
+    from coulomb_kmc_gb300.serving import default_r, system_inputs
+    if sample is None:
+        # the systems at the 30th and 70th percentile of N of each boundary condition
+        sample = []
+        for bc in ("free_space", "pbc"):
+            idx = sorted((i for i in range(len(reqs)) if reqs[i].bc == bc), key=lambda i: reqs[i].n)
+            sample += [idx[(3 * len(idx)) // 10], idx[(7 * len(idx)) // 10]]
+    systems = []
+    for i in sample:
+        r = reqs[i]
+        pos, q, E, _, _ = system_inputs(r)
+        R_ = default_r(len(q))
+        o = ko.OracleKMC(pos.copy(), q, E, R_, r.L, r.bc, max_move=C4_STEP,
+                         lr_operator=lattice_operator(r.L, E) if r.bc == "pbc" else None)
+        o.initialise(local_expansions=np.zeros(((2 ** (R_ - 1)) ** 3, 2 * r.L * r.L)))
+        systems.append((o, E))
+    rng = np.random.default_rng(5)
+
+    def one_round():
+        n_tot = 0
+        for o, E in systems:
+            n = o.N
+            prop = offlattice_proposals(o.positions, E, rng)
+            d = np.zeros((n, 1))
+            o.propose_with_dats(np.array([1], np.int64), np.zeros((n, 1), np.int64), prop,
+                                np.ones((n, 1), np.int64), d)
+            pid = int(rng.integers(0, n))
+            if rng.uniform() < np.exp(-C4_BETA * d[pid, 0]):
+                o.accept((pid, prop[pid].copy()))
+            n_tot += n
+        return n_tot
+
+    for _ in range(warmup):
+        one_round()
+    t0 = time.perf_counter()
+    nprop = sum(one_round() for _ in range(rounds))
+    dt = time.perf_counter() - t0
+    desc = (f"{rounds} Metropolis rounds of {len(sample)} of the {len(reqs)} systems (N = "
+            f"{', '.join(str(reqs[i].n) + ' ' + reqs[i].bc for i in sample)}; {nprop} proposals) on the oracle "
+            f"(restated reference CPU path, OpenMP {os.cpu_count()} threads; initial expansions zero, which does "
+            f"not change the operation count)")
+    return nprop / dt, dt, nprop, desc
+
+
+def bench_config1(args):
+    """Plain FP64 free space: N=1,000 charges in a box of edge 12 (seed 0), R=3, L=12;
+    every charge proposes one move per step (uniform in [-0.5, 0.5]^3), one random
+    charge's move accepted by Metropolis at beta = 1; 100 steps, device driver with a
+    captured step graph.  Also the mixed mode with FP64 accept contributions."""
+    import torch
+    from coulomb_kmc_gb300 import KMCFMM
+    from coulomb_kmc_gb300.dats import make_state
+    from coulomb_kmc_gb300.driver import KMCDriver
+    from coulomb_kmc_gb300.workloads import OffLatticeSystem
+    out = {}
+    for prec in ("fp64", "mixed_fp64_accept"):
+        hs = OffLatticeSystem(1000, 12.0, seed=0, step=0.5)
+        st = make_state(hs.positions(), hs.charges(), 12.0)
+        k = KMCFMM(st.P, st.Q, st.domain, r=3, l=12, boundary_condition="free_space", max_move=0.5,
+                   precision=prec)
+        k.initialise()
+        d = KMCDriver(k, "offlattice", 1.0, seed=1, step=0.5)
+        d.step(3)
+        d.capture()
+        torch.cuda.synchronize()
+        s0 = d.stats()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(d.stream)
+        d.launch(100, stream=d.stream)
+        e1.record(d.stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        s1 = d.stats()
+        out[prec] = {"value": (s1[2] - s0[2]) / (ms * 1e-3), "ms_per_step": ms / 100, "steps": 100,
+                     "accepted": s1[1] - s0[1]}
+        d.free()
+        k.free()
+    out["workload"] = ("free_space N=1000, box 12, seed 0, R=3, L=12, one proposal per charge per step, "
+                       "Metropolis beta=1, 100 steps")
+    return out
+
+
+def bench_config2_extra(args, rank, local):
+    """pbc lattice hopping on 48^3 sites (27,648 charges, R=5, L=12, rejection-free,
+    beta=2): the mixed mode with FP64 accept contributions, plain FP64 and the mixed mode
+    with double-FP32 accept contributions; errors against FP64."""
+    import torch
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    out = {}
+    for prec, nsteps in (("mixed_fp64_accept", args.steps), ("fp64", max(5, args.steps // 3)),
+                         ("mixed", args.steps)):
+        _, k, d, _ = make_system(SIDE, rank, prec, local)
+        ps, npr, _, _ = timed_loop(k, d, nsteps, 3, flush)
+        out[prec] = {"value": npr / (ps.sum() * 1e-3), "ms_per_step": float(ps.mean()),
+                     "p50_ms": float(np.percentile(ps, 50)), "p99_ms": float(np.percentile(ps, 99)),
+                     "steps": len(ps)}
+        d.free()
+        k.free()
+    out["mixed_fp64_accept"]["vs_fp64"] = out["mixed_fp64_accept"]["value"] / out["fp64"]["value"]
+    out["mixed"]["vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["error_mixed_fp64_accept"] = mixed_error_stats(SIDE, local, precision="mixed_fp64_accept")
+    out["error_mixed"] = mixed_error_stats(SIDE, local, precision="mixed")
+    out["workload"] = workload_config(SIDE, "mixed_fp64_accept")["workload"]
+    return out
+
+
+def run_reference_config4(args):
+    """--impl reference on the headline workload: the oracle restatement of the
+    reference's CPU path, each step one Metropolis round of a fixed sample of the
+    systems (bounded so that --steps K --warmup W ends within minutes)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = os.cpu_count()
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    reqs = config4_requests(args.systems)
+    v, dt, nprop, smp = cpu_config4(reqs, args.steps, args.warmup)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(args.steps, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config4_config(args, "fp64"),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": smp},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def config4_config(args, precision):
+    return {"workload": config4_workload(args.systems), "systems": args.systems, "L": 12, "precision": precision,
+            "rounds": args.steps, "l2": "inputs larger than L2: the systems' state (~1 GB over 256 systems) is "
+                                       "far above the 129 MB L2, no flush between rounds"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "mixed_fp64_accept", "fp64"])
+    ap.add_argument("--precision", default="mixed_fp64_accept", choices=["mixed", "mixed_fp64_accept", "fp64"])
     ap.add_argument("--side", type=int, default=SIDE)
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-steps", type=int, default=5)
+    ap.add_argument("--cpu-rounds", type=int, default=2)
+    ap.add_argument("--fp64-rounds", type=int, default=3)
+    ap.add_argument("--build-threads", type=int, default=4)
     ap.add_argument("--ref-steps", type=int, default=10)
     ap.add_argument("--no-extras", action="store_true", help="timed loop only (for profiler runs)")
     ap.add_argument("--no-graph", action="store_true", help="launch the step eagerly instead of a CUDA graph")
-    ap.add_argument("--workload", default="lattice48",
-                    choices=["lattice48", "precision_split", "batched", "serving", "drift"])
+    ap.add_argument("--workload", default="batched",
+                    choices=["batched", "lattice48", "precision_split", "batched_streams", "serving", "drift"])
     ap.add_argument("--accepts", type=int, nargs="+", default=[0, 2000, 10000, 30000])
     ap.add_argument("--fp32-from", type=int, default=None, help="drift: first accept order in FP32 (tuning key 6)")
     ap.add_argument("--orders", type=int, nargs="+", default=[8, 12, 16])
     ap.add_argument("--error-steps", type=int, default=3)
-    ap.add_argument("--systems", type=int, default=64)
+    ap.add_argument("--systems", type=int, default=256)
     ap.add_argument("--rounds", type=int, default=20)
     ap.add_argument("--workers", type=int, default=16)
     ap.add_argument("--requests", type=int, default=16)
@@ -571,16 +1059,17 @@ def main():
     ap.add_argument("--max-active", type=int, default=64)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
-    if args.workload != "lattice48" and args.impl == "ours":
+    if args.impl == "reference":
+        if args.workload == "batched":
+            run_reference_config4(args)
+        else:
+            run_reference(args)
+        return
+    if args.workload in ("precision_split", "batched_streams", "serving", "drift"):
         import torch
         torch.cuda.set_device(0)
-        {"precision_split": bench_precision_split, "batched": bench_batched, "serving": bench_serving,
-         "drift": bench_drift}[
-            args.workload](args)
-        return
-
-    if args.impl == "reference":
-        run_reference(args)
+        {"precision_split": bench_precision_split, "batched_streams": bench_batched, "serving": bench_serving,
+         "drift": bench_drift}[args.workload](args)
         return
 
     import torch
@@ -591,6 +1080,33 @@ def main():
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    if args.workload == "lattice48":
+        main_lattice48(args, world, rank, local)
+    else:
+        value, t_ms, nprop, ms, clk, launches, build_s, extras = bench_config4(args, rank, world, local)
+        if rank == 0:
+            dtype = {"fp64": "f64",
+                     "mixed": "f32+df32 (f64 master state, energy, lattice operator g, final difference)",
+                     "mixed_fp64_accept": "f32+df32 near field and harmonic evaluation; f64 accept increments, "
+                                          "lattice operator (g = A M, h = A b), energy and final difference"}[
+                args.precision]
+            line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                    "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
+                    "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+                    "config": dict(config4_config(args, args.precision), proposals_per_round=nprop / args.steps,
+                                   replicas=world, build_s=build_s),
+                    "p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99)),
+                    "clocks": clk, "gpu_launches": int(launches * args.steps) if launches else None,
+                    "cuda_graph": True}
+            line.update(extras)
+            print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main_lattice48(args, world, rank, local):
+    import torch
+    import torch.distributed as dist
     from coulomb_kmc_gb300 import KMCFMM, _native
     from coulomb_kmc_gb300.dats import make_state
     from coulomb_kmc_gb300.workloads import LatticeHopSystem
@@ -642,6 +1158,7 @@ def main():
             "bound": bound, "kernel": top, "achieved": ach.get(top), "peak": peak, "unit": "TFLOP/s",
             "frac": (ach.get(top) / peak) if ach.get(top) else None,
             "traffic": NCU_TRAFFIC.get(top) if args.precision == "fp64" else NCU_TRAFFIC_MIXED.get(top),
+            "traffic_source": NCU_SOURCE, "issue_frac_source": NCU_SOURCE,
             "peak_source": "measured in this run with kmc_diag_fma_rate (FMA issue rate of the FP64 / FP32 "
                            "pipe); MEASURED_PEAKS.json holds HBM and bf16 only, and these kernels are "
                            "arithmetic bound with an L2-resident state",
@@ -723,8 +1240,8 @@ def main():
                 "cuda_graph": not args.no_graph}
         line.update(extras)
         print(json.dumps(line))
-    if world > 1:
-        dist.destroy_process_group()
+
+
 
 
 if __name__ == "__main__":

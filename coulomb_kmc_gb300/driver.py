@@ -47,6 +47,7 @@ class KMCDriver:
             prm.lattice_side = int(lattice_side)
             prm.lattice_sites = sites.ctypes.data_as(POINTER(c_int64))
         self._handle = c_void_p()
+        kmc._set_stream()  # set-up work on the caller's current stream
         _native.check(_native.lib().kmc_driver_create(kmc._handle, byref(prm), byref(self._handle)),
                       "kmc_driver_create")
         self.log_capacity = int(log_capacity)

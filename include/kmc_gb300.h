@@ -249,7 +249,7 @@ int kmc_inject(kmc_system *s, int64_t n, const double *positions, const double *
 #define KMC_TUNE_FSELF_GENERIC 8 /* mixed pbc lattice self term: 0 unrolled L = 12 cubic evaluator, 1 interpreter */
 #define KMC_TUNE_P2L_PAIR 9 /* double-FP32 accept at L = 12, orders from 6 in FP32: 0 column-pair kernel, 1 per-column kernel */
 #define KMC_TUNE_P2L64 10 /* FP64 accept at L = 8, 12, 16: 0 column-pair kernel, 1 per-column kernel */
-#define KMC_TUNE_P2L64_GROUPS 11 /* FP64 column-pair accept: k source-group pairs, 2k groups (1..4; 0: 4 groups) */
+#define KMC_TUNE_P2L64_CELLS 11 /* FP64 column-pair accept: cells per block, 1, 2, 4, 8 or 16 (0: 2); 32 / cells source groups */
 #define KMC_NTUNE 12
 int kmc_set_tuning(kmc_system *s, int32_t key, int32_t value);
 int kmc_get_tuning(kmc_system *s, int32_t key, int32_t *value_out);
