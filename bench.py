@@ -639,31 +639,63 @@ class HostRound:
         self.proposals = 0
         self.h2d = 0
         self.d2h = 0
+        self.phase = {"host_proposals": 0.0, "propose_with_dats": 0.0, "select_accept": 0.0}
 
     def run(self, kmc_list=None):
+        pc = time.perf_counter
         for (k, E), (smc, sites, masks, diffs) in zip(self.kmcs, self.buf):
+            t0 = pc()
             pos = k.positions if isinstance(k.positions, np.ndarray) else np.asarray(k._positions_host())
             prop = offlattice_proposals(np.asarray(pos, dtype=np.float64).reshape(-1, 3), E, self.rng)
+            t1 = pc()
             k.propose_with_dats(smc, sites, prop, masks, diffs)
+            t2 = pc()
             pid = int(self.rng.integers(0, k.N))
             if self.rng.uniform() < np.exp(-C4_BETA * diffs[pid, 0]):
                 k.accept((pid, prop[pid].copy()))
+            t3 = pc()
+            self.phase["host_proposals"] += t1 - t0
+            self.phase["propose_with_dats"] += t2 - t1
+            self.phase["select_accept"] += t3 - t2
             self.proposals += k.N
             self.h2d += smc.nbytes + sites.nbytes + prop.nbytes + masks.nbytes + diffs.nbytes
             self.d2h += diffs.nbytes + 16
 
 
-def make_slots(reqs, kmcs):
+def make_slots(reqs, kmcs, autotune=False):
+    """A device driver per system; with `autotune`, the launch shapes of each size
+    bucket (depth, order, boundary condition) are tuned on its largest system
+    (kmc_autotune: only variants that leave every result bit-identical) and applied
+    to all its systems; then every step is captured.  Returns (slots, choices)."""
+    import torch
     from coulomb_kmc_gb300.driver import KMCDriver
-    from coulomb_kmc_gb300.serving import Slot
+    from coulomb_kmc_gb300.serving import Server, Slot
     slots = []
     for r, (k, E) in zip(reqs, kmcs):
         d = KMCDriver(k, "offlattice", C4_BETA, seed=r.seed, step=C4_STEP)
-        d.capture()
         slots.append(Slot(req=r, kmc=k, drv=d, nbytes=0, admitted=0.0))
-    import torch
+    choices = {}
+    if autotune:
+        buckets = {}
+        for sl in slots:
+            buckets.setdefault(Server.bucket_key(sl), []).append(sl)
+        for key, members in sorted(buckets.items()):
+            big = max(members, key=lambda sl: sl.kmc.N)
+            big.drv.step(1)  # a proposal set-up for the lattice kernels to run on
+            torch.cuda.synchronize()
+            with torch.cuda.stream(big.drv.stream):
+                tuned = big.kmc.autotune(reps=5)
+            torch.cuda.synchronize()
+            big.kmc._set_stream()
+            picked = {k: v for k, v in tuned.items() if v}
+            for sl in members:
+                for k, v in picked.items():
+                    sl.kmc.set_tuning(k, v)
+            choices["R=%d L=%d %s %s" % key] = picked
+    for sl in slots:
+        sl.drv.capture()
     torch.cuda.synchronize()
-    return slots
+    return slots, choices
 
 
 def timed_rounds(srv, slots, steps, warmup, sampler=None):
@@ -800,6 +832,7 @@ def bench_config4(args, rank, world, local):
         hr.run()
         torch.cuda.synchronize()
         p0, b0, c0 = hr.proposals, hr.h2d, hr.d2h
+        ph0 = dict(hr.phase)
         t1 = time.perf_counter()
         for _ in range(args.e2e_steps):
             hr.run()
@@ -809,12 +842,17 @@ def bench_config4(args, rank, world, local):
         extras["e2e"] = {"value": (hr.proposals - p0) / e2e_dt, "unit": UNIT,
                          "h2d_bytes_per_step": int((hr.h2d - b0) / nr), "d2h_bytes_per_step": int((hr.d2h - c0) / nr),
                          "steps": args.e2e_steps,
+                         "phases_s_per_round": {k: (hr.phase[k] - ph0[k]) / nr for k in hr.phase},
                          "path": "KMCFMM.propose_with_dats with numpy buffers (pinned staging, H2D of every "
                                  "proposal array, D2H of the differences) + host Metropolis + KMCFMM.accept, "
                                  "every system every round"}
-    slots = make_slots(reqs, kmcs)
+    slots, tuned = make_slots(reqs, kmcs, autotune=True)
     launches = launches_per_step(slots) if not args.no_extras else None
     srv = Server(precision=prec, n_workers=args.workers)
+    # the round's launch structure (per-system graphs on worker streams, or one graph per
+    # size bucket): both timed over a few rounds (untimed warm-up rounds), the faster kept
+    mode, mode_ms = srv.autotune_launch(slots, rounds=3)
+    extras["autotune"] = {"kernel_launch_shapes": tuned, "round_launch": mode, "round_ms_by_launch": mode_ms}
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
@@ -848,6 +886,7 @@ def bench_config4(args, rank, world, local):
             fl, mnb = offlattice_flop_model(sl.kmc, 12)
             big[bc] = {"n": reqs[i].n, "per_kernel_ms": {k: round(v, 5) for k, v in per_launch.items()},
                        "near_flops": fl, "mean_neighbours": mnb}
+        srv.free_buckets()
         free_slots(slots)
         peak64, peak32 = fma_peak(True), fma_peak(False)
         b = big["pbc"]
@@ -868,12 +907,15 @@ def bench_config4(args, rank, world, local):
                             "DRAM bytes per launch"}
         # the plain FP64 path on the same systems
         k64 = build_kmcs(reqs, "fp64", threads=args.build_threads)
-        s64 = make_slots(reqs, k64)
+        s64, _ = make_slots(reqs, k64)
         srv64 = Server(precision="fp64", n_workers=args.workers)
-        ms64, np64, _ = timed_rounds(srv64, s64, max(2, args.fp64_rounds), 1)
+        mode64, _ = srv64.autotune_launch(s64, rounds=1)
+        ms64, np64, _ = timed_rounds(srv64, s64, max(2, args.fp64_rounds), 0)
+        srv64.free_buckets()
         free_slots(s64)
         extras["fp64"] = {"value": np64 / (ms64.sum() * 1e-3), "round_ms_p50": float(np.percentile(ms64, 50)),
-                          "round_ms_p99": float(np.percentile(ms64, 99)), "rounds": len(ms64)}
+                          "round_ms_p99": float(np.percentile(ms64, 99)), "rounds": len(ms64),
+                          "round_launch": mode64}
         extras["mixed_vs_fp64"] = value / extras["fp64"]["value"]
         print(json.dumps({"stage": "fp64", **extras["fp64"]}), file=sys.stderr, flush=True)
         extras["mixed_error"] = config4_error_stats(reqs)
@@ -884,6 +926,7 @@ def bench_config4(args, rank, world, local):
         extras["config1"] = bench_config1(args)
         extras["config2"] = bench_config2_extra(args, rank, local)
     else:
+        srv.free_buckets()
         free_slots(slots)
     return value, t_ms, nprop, ms, clk, launches, build_s, extras
 

@@ -50,6 +50,9 @@ class KmcDriverParams(ctypes.Structure):
 
 
 KMC_DRIVE = {"lattice": 0, "offlattice": 1}
+# tuning keys (include/kmc_gb300.h)
+KMC_TUNE_P2L64_CELLS = 11
+KMC_TUNE_LR_THREADS = 12
 
 
 def _nvcc():
@@ -109,6 +112,10 @@ SIGNATURES = {
     "kmc_inject": ([c_void_p, c_int64, c_void_p, c_void_p, POINTER(c_double)], c_int),
     "kmc_set_tuning": ([c_void_p, c_int32, c_int32], c_int),
     "kmc_get_tuning": ([c_void_p, c_int32, POINTER(c_int32)], c_int),
+    "kmc_autotune": ([c_void_p, c_int32, c_void_p], c_int),
+    "kmc_bucket_create": ([c_void_p, c_int64, POINTER(c_void_p)], c_int),
+    "kmc_bucket_launch": ([c_void_p, c_int64, c_void_p], c_int),
+    "kmc_bucket_free": ([c_void_p], c_int),
     "kmc_driver_create": ([c_void_p, POINTER(KmcDriverParams), POINTER(c_void_p)], c_int),
     "kmc_driver_step": ([c_void_p, c_int64], c_int),
     "kmc_driver_capture": ([c_void_p], c_int),
@@ -170,6 +177,7 @@ class DedicatedStream:
 
 
 NKERNELS = 18
+NTUNE = 13
 
 
 def check(rc, what):

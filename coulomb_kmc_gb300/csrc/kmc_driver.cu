@@ -427,6 +427,7 @@ struct kmc_driver {
     // the store has slots)
     int64_t budget = 0;
     int64_t layout = -1;            // the system's buffer layout the captured graph reads
+    int64_t graph_version = 0;      // advances at every capture (size-bucket graphs embed the step)
     cudaEvent_t ev_last = nullptr;  // after the driver's last enqueued step
     bool ev_recorded = false;
     cudaStream_t own_stream = nullptr;  // for re-capturing the step after a store growth
@@ -763,6 +764,7 @@ int capture_core(kmc_driver *d, cudaStream_t st)
     d->graph = g;
     if (cudaGraphInstantiate(&d->exec, g, 0) != cudaSuccess) return KMC_ECUDA;
     d->layout = kmc_int_layout_gen(d->sys);
+    d->graph_version++;
     return KMC_OK;
 }
 
@@ -911,5 +913,89 @@ int kmc_drivers_launch(kmc_driver **drivers, int64_t n, int64_t steps, void *mai
         DRV_CUDA(cudaEventRecord(ev[w + 1], (cudaStream_t)worker_streams[w]));
         DRV_CUDA(cudaStreamWaitEvent(ms, ev[w + 1], 0));
     }
+    return KMC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Size buckets: one CUDA graph holding the captured steps of many systems (child
+// graph nodes with no edges between them, so the systems' steps run concurrently
+// as the device has room), launched once per round instead of once per system.
+// The child graphs are copies: when a member captures its step again (a store
+// growth, a new tuning), the bucket graph is rebuilt before its next launch.
+// ---------------------------------------------------------------------------
+struct kmc_bucket {
+    std::vector<kmc_driver *> drv;
+    std::vector<int64_t> versions;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+int bucket_build(kmc_bucket *b)
+{
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    if (b->graph) {
+        cudaGraphDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    DRV_CUDA(cudaGraphCreate(&b->graph, 0));
+    b->versions.resize(b->drv.size());
+    for (size_t i = 0; i < b->drv.size(); ++i) {
+        cudaGraphNode_t node;
+        DRV_CUDA(cudaGraphAddChildGraphNode(&node, b->graph, nullptr, 0, b->drv[i]->graph));
+        b->versions[i] = b->drv[i]->graph_version;
+    }
+    DRV_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+    return KMC_OK;
+}
+} // namespace
+
+int kmc_bucket_create(kmc_driver **drivers, int64_t n, kmc_bucket **out)
+{
+    if (!drivers || n <= 0 || !out) return KMC_EINVAL;
+    *out = nullptr;
+    for (int64_t i = 0; i < n; ++i)
+        if (!drivers[i] || !drivers[i]->graph) return KMC_ESTATE;
+    kmc_bucket *b = new (std::nothrow) kmc_bucket;
+    if (!b) return KMC_ENOMEM;
+    b->drv.assign(drivers, drivers + n);
+    const int rc = bucket_build(b);
+    if (rc) {
+        kmc_bucket_free(b);
+        return rc;
+    }
+    *out = b;
+    return KMC_OK;
+}
+
+int kmc_bucket_launch(kmc_bucket *b, int64_t steps, void *stream)
+{
+    if (!b || steps < 0) return KMC_EINVAL;
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc;
+    bool stale = false;
+    for (size_t i = 0; i < b->drv.size(); ++i) {
+        kmc_driver *d = b->drv[i];
+        if ((rc = ensure_headroom(d, steps))) return rc;
+        if (d->graph_pipelined && (rc = ensure_prepared(d, st))) return rc;
+        stale = stale || d->graph_version != b->versions[i];
+    }
+    if (stale && (rc = bucket_build(b))) return rc;
+    for (int64_t k = 0; k < steps; ++k) DRV_CUDA(cudaGraphLaunch(b->exec, st));
+    if (steps > 0)
+        for (kmc_driver *d : b->drv)
+            if ((rc = mark_enqueued(d, st))) return rc;
+    return KMC_OK;
+}
+
+int kmc_bucket_free(kmc_bucket *b)
+{
+    if (!b) return KMC_EINVAL;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    delete b;
     return KMC_OK;
 }

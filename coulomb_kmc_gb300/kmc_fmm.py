@@ -330,6 +330,20 @@ class KMCFMM:
                                                       d_energy_diff.data_ptr()), "kmc_accept_device")
         self._energy_valid = False
 
+    def autotune(self, reps=5):
+        """Time the launch-shape candidates that leave every result bit-identical and keep
+        the fastest (kmc_autotune); returns {key: value} of all tuning keys.  The lattice
+        kernels are tuned on the proposals of the last propose, so call it after one."""
+        self._assert_init()
+        self._set_stream()
+        out = (ctypes.c_int32 * _native.NTUNE)()
+        _native.check(_native.lib().kmc_autotune(self._handle, int(reps), out), "kmc_autotune")
+        return {k: int(out[k]) for k in range(_native.NTUNE)}
+
+    def set_tuning(self, key, value):
+        """Set one launch-shape tuning key (kmc_set_tuning)."""
+        _native.check(_native.lib().kmc_set_tuning(self._handle, int(key), int(value)), "kmc_set_tuning")
+
     def reserve_store(self, capacity):
         """Set the cell store's capacity (slots per cell) to at least ``capacity`` and the
         largest occupancy (kmc_store_reserve); returns the new capacity.  Synchronises; a

@@ -17,6 +17,7 @@ systems advancing one step) is timed with CUDA events.  Nothing here changes
 results: a system evolves identically alone or in any mix (deterministic
 kernels, per-system Philox streams).
 """
+import ctypes
 import math
 import queue
 import threading
@@ -128,9 +129,18 @@ class _null:
 
 class Server:
     def __init__(self, precision="mixed", hbm_budget=150e9, max_active=64, n_workers=16, keep_results=False,
-                 n_admit=4):
+                 n_admit=4, launch="streams"):
         import torch
+        if launch not in ("streams", "buckets"):
+            raise ValueError("launch must be 'streams' or 'buckets'")
         self.precision = precision
+        # how a round is launched: "streams" -- every system's captured step graph on one of
+        # the worker streams; "buckets" -- one graph per size bucket holding the steps of
+        # all its systems (kmc_bucket_*), the buckets spread over the worker streams.
+        # Results are the same either way (the same step graphs run); autotune_launch()
+        # times both and keeps the faster.
+        self.launch = launch
+        self._buckets = {}  # bucket key -> (driver handles, kmc_bucket handle)
         self.keep_results = bool(keep_results)
         self.results = {}
         self.peak_active = 0
@@ -160,21 +170,81 @@ class Server:
         self._e1 = torch.cuda.Event(enable_timing=True)
 
     # -- one round over the given slots ------------------------------------
+    @staticmethod
+    def bucket_key(slot):
+        """Size bucket of a system: the same FMM depth, order, boundary condition and
+        kind of driver (the same kernels and launch shapes)."""
+        return (slot.kmc.R, slot.kmc.L, str(slot.req.bc), slot.req.kind)
+
+    def _bucket_handles(self, slots):
+        """One kmc_bucket per size bucket of `slots` (kept while its members stay)."""
+        groups = {}
+        for sl in slots:
+            groups.setdefault(self.bucket_key(sl), []).append(sl.drv._handle.value)
+        out = []
+        for key, members in sorted(groups.items()):
+            members = tuple(members)
+            have = self._buckets.get(key)
+            if have is None or have[0] != members:
+                if have is not None:
+                    _native.lib().kmc_bucket_free(have[1])
+                arr = (c_void_p * len(members))(*members)
+                h = c_void_p()
+                _native.check(_native.lib().kmc_bucket_create(arr, len(members), ctypes.byref(h)),
+                              "kmc_bucket_create")
+                self._buckets[key] = (members, h)
+            out.append(self._buckets[key][1])
+        for key in [k for k in self._buckets if k not in groups]:
+            _native.lib().kmc_bucket_free(self._buckets.pop(key)[1])
+        return out
+
+    def free_buckets(self):
+        for _, h in self._buckets.values():
+            _native.lib().kmc_bucket_free(h)
+        self._buckets = {}
+
     def round(self, slots):
         """Advance every slot one step; returns the round's device time in ms."""
         import torch
         if not slots:
             return 0.0
-        arr = (c_void_p * len(slots))(*[s.drv._handle.value for s in slots])
         e0, e1 = self._e0, self._e1
-        e0.record(self.main)
-        _native.check(self._launch(arr, len(slots), 1, c_void_p(self.main.cuda_stream), self._worker_ptrs,
-                                   len(self.workers)), "kmc_drivers_launch")
+        if self.launch == "buckets":
+            hs = self._bucket_handles(slots)
+            e0.record(self.main)
+            for i, h in enumerate(hs):
+                w = self.workers[i % len(self.workers)]
+                w.wait_event(e0)
+                _native.check(_native.lib().kmc_bucket_launch(h, 1, c_void_p(w.cuda_stream)), "kmc_bucket_launch")
+            for w in self.workers[:len(hs)]:
+                self.main.wait_stream(w)
+        else:
+            arr = (c_void_p * len(slots))(*[s.drv._handle.value for s in slots])
+            e0.record(self.main)
+            _native.check(self._launch(arr, len(slots), 1, c_void_p(self.main.cuda_stream), self._worker_ptrs,
+                                       len(self.workers)), "kmc_drivers_launch")
         e1.record(self.main)
         e1.synchronize()
         for s in slots:
             s.done += 1
         return e0.elapsed_time(e1)
+
+    def autotune_launch(self, slots, rounds=3):
+        """Time `rounds` rounds with each launch structure and keep the faster (the
+        rounds are real rounds: every system advances, identically in either mode)."""
+        best = None
+        timing = {}
+        for mode in ("streams", "buckets"):
+            self.launch = mode
+            self.round(slots)  # the first round of a mode builds its graphs
+            ms = float(np.median([self.round(slots) for _ in range(rounds)]))
+            timing[mode] = ms
+            if best is None or ms < timing[best]:
+                best = mode
+        self.launch = best
+        if best != "buckets":
+            self.free_buckets()
+        return best, timing
 
     def admit(self, req, stream=None):
         t0 = time.perf_counter()
@@ -342,6 +412,7 @@ class Server:
                         graveyard.put(s)
             ok = True
         finally:
+            self.free_buckets()
             stop.set()
             for th in threads:
                 th.join(timeout=60)

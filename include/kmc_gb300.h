@@ -235,9 +235,7 @@ int kmc_extract(kmc_system *s, int64_t n, const int64_t *ids, double *de_out);
 int kmc_inject(kmc_system *s, int64_t n, const double *positions, const double *charges, double *de_out);
 
 /* Launch-shape tuning (no reference counterpart; the reference has fixed
- * OpenMP loops).  key: KMC_TUNE_*; value 0 restores the built-in choice.
- * kmc_autotune times the candidates of every key on scratch buffers of this
- * handle (the handle's state is not changed) and keeps the fastest. */
+ * OpenMP loops).  key: KMC_TUNE_*; value 0 restores the built-in choice. */
 #define KMC_TUNE_P2L_GROUPS 0 /* source groups per block of the double-FP32 accept kernel (1..4) */
 #define KMC_TUNE_LR_FUSED 1   /* mixed pbc lattice term: 0 per-charge and per-proposal kernels, 1 one fused kernel */
 #define KMC_TUNE_LR_STAGE 2   /* fused lattice kernel: 0 folded form in shared memory (when it fits), 1 read-only cache */
@@ -249,10 +247,20 @@ int kmc_inject(kmc_system *s, int64_t n, const double *positions, const double *
 #define KMC_TUNE_FSELF_GENERIC 8 /* mixed pbc lattice self term: 0 unrolled L = 12 cubic evaluator, 1 interpreter */
 #define KMC_TUNE_P2L_PAIR 9 /* double-FP32 accept at L = 12, orders from 6 in FP32: 0 column-pair kernel, 1 per-column kernel */
 #define KMC_TUNE_P2L64 10 /* FP64 accept at L = 8, 12, 16: 0 column-pair kernel, 1 per-column kernel */
-#define KMC_TUNE_P2L64_CELLS 11 /* FP64 column-pair accept: cells per block, 1, 2, 4, 8 or 16 (0: 2); 32 / cells source groups */
-#define KMC_NTUNE 12
+#define KMC_TUNE_P2L64_CELLS 11 /* FP64 column-pair accept: cells per block, 2, 4 or 8 (0: 2) */
+#define KMC_TUNE_LR_THREADS 12 /* mixed pbc per-proposal lattice kernels: threads per block, 64, 128 or 256 (0: 128) */
+#define KMC_NTUNE 13
 int kmc_set_tuning(kmc_system *s, int32_t key, int32_t value);
 int kmc_get_tuning(kmc_system *s, int32_t key, int32_t *value_out);
+/* Autotuner (no reference counterpart; the reference's OpenMP loops and block-256
+ * CUDA launches are fixed): times `reps` launches of each candidate of the keys
+ * whose variants give bit-identical results -- KMC_TUNE_LR_THREADS (after a
+ * proposal set-up, mixed pbc) and KMC_TUNE_P2L64_CELLS (FP64 accept) -- on this
+ * handle and keeps the fastest.  The state is not changed: the lattice kernels
+ * rerun the last set-up's proposals into proposal scratch, the accept kernel runs
+ * on a copy of the expansions.  chosen_out (may be NULL) receives all KMC_NTUNE
+ * values.  Synchronises; allocates scratch for the call. */
+int kmc_autotune(kmc_system *s, int32_t reps, int32_t *chosen_out);
 
 /* ------------------------------------------------------------------------
  * Device-side KMC driver: proposal generation, selection and lattice
@@ -302,6 +310,19 @@ int kmc_driver_free(kmc_driver *d);
  * waits for all of them.  No host synchronisation.  Call from one host thread. */
 int kmc_drivers_launch(kmc_driver **drivers, int64_t n, int64_t steps, void *main_stream, void **worker_streams,
                        int64_t n_workers);
+
+/* Size buckets (no reference counterpart): one CUDA graph holding the captured
+ * steps of n drivers (typically systems of one size class: the same depth, order
+ * and boundary condition) as independent child graphs, so that one launch runs a
+ * round of all of them and the device overlaps their kernels as it has room.
+ * kmc_bucket_launch replays it `steps` times on `stream` after each member's
+ * store headroom check (a member that grows its store and captures its step again
+ * makes the bucket rebuild its graph first).  Results are those of the members'
+ * own launches.  The drivers must outlive the bucket. */
+typedef struct kmc_bucket kmc_bucket;
+int kmc_bucket_create(kmc_driver **drivers, int64_t n, kmc_bucket **out);
+int kmc_bucket_launch(kmc_bucket *b, int64_t steps, void *stream);
+int kmc_bucket_free(kmc_bucket *b);
 
 /* A dedicated non-blocking CUDA stream, not taken from any library's stream pool
  * (pooled streams are handed out round-robin and can alias, which breaks stream

@@ -1,0 +1,91 @@
+"""Launch-shape tuning and size-bucket launches change no result.
+
+* Every candidate of the keys the autotuner searches (proposals per block of the
+  per-proposal lattice kernels, cells per block of the FP64 accept kernel) gives
+  the same selections, positions, energy and expansions, bit for bit, as the
+  built-in choice, over a chain of device-driven KMC steps; so does whatever
+  kmc_autotune picks.
+* A round launched as size-bucket graphs (one graph per bucket holding every
+  member's captured step) leaves every system exactly as the per-system stream
+  launches do.
+"""
+import numpy as np
+import pytest
+
+from coulomb_kmc_gb300 import KMCFMM, _native
+from coulomb_kmc_gb300.dats import make_state
+from coulomb_kmc_gb300.driver import KMCDriver
+from coulomb_kmc_gb300.serving import Request, Server, Slot, build_system
+from coulomb_kmc_gb300.workloads import LatticeHopSystem
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(tune=None, autotune=False, steps=12):
+    hs = LatticeHopSystem(side=24, occupancy=0.25, seed=5)
+    st = make_state(hs.positions(), hs.charges(), hs.extent)
+    k = KMCFMM(st.P, st.Q, st.domain, r=4, l=12, boundary_condition="pbc", max_move=1.0,
+               precision="mixed_fp64_accept")
+    k.initialise()
+    d = KMCDriver(k, "lattice", 2.0, seed=31, lattice_side=hs.side, lattice_sites=hs.site_of, log_capacity=64)
+    d.step(1)
+    chosen = None
+    if autotune:
+        chosen = k.autotune(reps=3)
+    for key, val in (tune or {}).items():
+        k.set_tuning(key, val)
+    d.capture()
+    d.launch(steps)
+    out = (d.log(), k.energy, k.state())
+    d.free()
+    k.free()
+    return out, chosen
+
+
+def _same(a, b):
+    (la, ea, sa), (lb, eb, sb) = a, b
+    for x, y in zip(la, lb):
+        assert np.array_equal(x, y)
+    assert ea == eb
+    assert np.array_equal(sa["positions"], sb["positions"])
+    assert np.array_equal(sa["local_expansions"], sb["local_expansions"])
+
+
+def test_every_tuning_candidate_is_bit_identical():
+    ref, _ = _run()
+    for val in (64, 256):
+        got, _ = _run({_native.KMC_TUNE_LR_THREADS: val})
+        _same(ref, got)
+    for val in (4, 8):
+        got, _ = _run({_native.KMC_TUNE_P2L64_CELLS: val})
+        _same(ref, got)
+
+
+def test_autotuned_choice_is_bit_identical():
+    ref, _ = _run()
+    got, chosen = _run(autotune=True)
+    assert chosen[_native.KMC_TUNE_LR_THREADS] in (0, 64, 256)
+    assert chosen[_native.KMC_TUNE_P2L64_CELLS] in (0, 4, 8)
+    _same(ref, got)
+
+
+def test_bucket_rounds_equal_stream_rounds():
+    reqs = [Request(rid=i, kind="offlattice" if i % 2 else "lattice", bc="free_space" if i % 2 else "pbc",
+                    n=1200 + 300 * (i % 3), rounds=6, seed=40 + i) for i in range(8)]
+    res = {}
+    for mode in ("streams", "buckets"):
+        srv = Server(precision="mixed_fp64_accept", n_workers=4, launch=mode)
+        slots = []
+        for r in reqs:
+            k, d = build_system(r, "mixed_fp64_accept")
+            slots.append(Slot(req=r, kmc=k, drv=d, nbytes=0, admitted=0.0))
+        for _ in range(6):
+            srv.round(slots)
+        res[mode] = [(sl.kmc.energy, sl.drv.stats(), sl.kmc.state()["positions"]) for sl in slots]
+        srv.free_buckets()
+        for sl in slots:
+            sl.drv.free()
+            sl.kmc.free()
+    for a, b in zip(res["streams"], res["buckets"]):
+        assert a[0] == b[0] and a[1] == b[1]
+        assert np.array_equal(a[2], b[2])
