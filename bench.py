@@ -35,6 +35,7 @@ Other workloads (--workload; each prints its own JSON line):
   serving         : Poisson request stream through the continuous-batching
                     server, p50/p99 round latency and throughput, against FP64
                     one system at a time.
+  single          : one system (--case) stepped by its driver, for profiler captures.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload ...]
 Multi-GPU (torchrun): independent replicas, no collective on the data path; value =
@@ -612,11 +613,12 @@ def build_kmcs(reqs, precision, threads=4):
     return out
 
 
-def offlattice_proposals(pos, E, rng):
+def offlattice_proposals(pos, E, rng, out=None):
     """One displacement per charge, uniform in [-step, step]^3, re-drawn (the same draws
-    in the same order) for the rows that left the box; only those rows are re-checked."""
+    in the same order) for the rows that left the box; only those rows are re-checked.
+    `out`: an (N, 3) array to write into."""
     h = 0.5 * E
-    prop = pos + rng.uniform(-C4_STEP, C4_STEP, size=pos.shape)
+    prop = np.add(pos, rng.uniform(-C4_STEP, C4_STEP, size=pos.shape), out=out)
     bad = np.flatnonzero(np.any(np.abs(prop) > h, axis=1))
     while bad.size:
         prop[bad] = pos[bad] + rng.uniform(-C4_STEP, C4_STEP, size=(bad.size, 3))
@@ -636,8 +638,12 @@ class HostRound:
         self.buf = []
         for k, E in kmcs:
             n = k.N
-            self.buf.append((np.array([1], np.int64), np.zeros((n, 1), np.int64), np.ones((n, 1), np.int64),
-                             np.zeros((n, 1))))
+            # the library's pinned host arrays, filled in place (no staging copies)
+            hb = k.host_buffers(1)
+            hb["current_sites"][:] = 0
+            hb["prop_masks"][:] = 1
+            self.buf.append((np.array([1], np.int64), hb["current_sites"], hb["prop_masks"],
+                             hb["prop_energy_diffs"], hb["prop_positions"]))
         self.proposals = 0
         self.h2d = 0
         self.d2h = 0
@@ -645,10 +651,10 @@ class HostRound:
 
     def run(self, kmc_list=None):
         pc = time.perf_counter
-        for (k, E), (smc, sites, masks, diffs) in zip(self.kmcs, self.buf):
+        for (k, E), (smc, sites, masks, diffs, prop) in zip(self.kmcs, self.buf):
             t0 = pc()
             pos = k.positions if isinstance(k.positions, np.ndarray) else np.asarray(k._positions_host())
-            prop = offlattice_proposals(np.asarray(pos, dtype=np.float64).reshape(-1, 3), E, self.rng)
+            offlattice_proposals(np.asarray(pos, dtype=np.float64).reshape(-1, 3), E, self.rng, out=prop)
             t1 = pc()
             k.propose_with_dats(smc, sites, prop, masks, diffs)
             t2 = pc()
@@ -1048,6 +1054,38 @@ def bench_config2_extra(args, rank, local):
     return out
 
 
+def bench_single(args):
+    """One system of a named case stepped by its device driver, for profiler captures of
+    single kernels (small enough for a full metric set): 'c4pbc' / 'c4free', the largest
+    pbc / free-space system of the batched workload; 'lattice48', the 48^3 lattice-hop
+    workload.  Prints the mean step time; the steps sit in an NVTX range 'steps'."""
+    import torch
+    from coulomb_kmc_gb300.driver import KMCDriver
+    if args.case in ("c4pbc", "c4free"):
+        reqs = config4_requests(args.systems)
+        bc = "pbc" if args.case == "c4pbc" else "free_space"
+        big = max((r for r in reqs if r.bc == bc), key=lambda r: r.n)
+        (k, E), = build_kmcs([big], args.precision, threads=1)
+        d = KMCDriver(k, "offlattice", C4_BETA, seed=big.seed, step=C4_STEP)
+        what = f"{bc} off-lattice N={big.n}"
+    else:
+        _, k, d, _ = make_system(SIDE, 0, args.precision, 0)
+        what = f"pbc lattice-hop {SIDE}^3"
+    d.step(2)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("steps")
+    e0.record(d.stream)
+    d.step(args.steps)
+    e1.record(d.stream)
+    e1.synchronize()
+    torch.cuda.nvtx.range_pop()
+    print(json.dumps({"workload": "single", "case": what, "precision": args.precision,
+                      "ms_per_step": e0.elapsed_time(e1) / max(args.steps, 1), "steps": args.steps}))
+    d.free()
+    k.free()
+
+
 def run_reference_config4(args):
     """--impl reference on the headline workload: the oracle restatement of the
     reference's CPU path, each step one Metropolis round of a fixed sample of the
@@ -1091,7 +1129,10 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="timed loop only (for profiler runs)")
     ap.add_argument("--no-graph", action="store_true", help="launch the step eagerly instead of a CUDA graph")
     ap.add_argument("--workload", default="batched",
-                    choices=["batched", "lattice48", "precision_split", "batched_streams", "serving", "drift"])
+                    choices=["batched", "lattice48", "precision_split", "batched_streams", "serving", "drift",
+                             "single"])
+    ap.add_argument("--case", default="c4pbc", choices=["c4pbc", "c4free", "lattice48"],
+                    help="single: the system to step")
     ap.add_argument("--accepts", type=int, nargs="+", default=[0, 2000, 10000, 30000])
     ap.add_argument("--fp32-from", type=int, default=None, help="drift: first accept order in FP32 (tuning key 6)")
     ap.add_argument("--orders", type=int, nargs="+", default=[8, 12, 16])
@@ -1112,11 +1153,11 @@ def main():
         else:
             run_reference(args)
         return
-    if args.workload in ("precision_split", "batched_streams", "serving", "drift"):
+    if args.workload in ("precision_split", "batched_streams", "serving", "drift", "single"):
         import torch
         torch.cuda.set_device(0)
         {"precision_split": bench_precision_split, "batched_streams": bench_batched, "serving": bench_serving,
-         "drift": bench_drift}[args.workload](args)
+         "drift": bench_drift, "single": bench_single}[args.workload](args)
         return
 
     import torch

@@ -53,6 +53,7 @@ KMC_DRIVE = {"lattice": 0, "offlattice": 1}
 # tuning keys (include/kmc_gb300.h)
 KMC_TUNE_P2L64_CELLS = 11
 KMC_TUNE_LR_THREADS = 12
+KMC_TUNE_NEAR_SPLIT = 13
 
 
 def _nvcc():
@@ -177,7 +178,7 @@ class DedicatedStream:
 
 
 NKERNELS = 18
-NTUNE = 13
+NTUNE = 14
 
 
 def check(rc, what):

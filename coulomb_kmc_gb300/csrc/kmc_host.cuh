@@ -1041,18 +1041,21 @@ int propose_evaluate(kmc_system *s, int64_t n_old_grid, int64_t n_new_grid, doub
             chunk * (2 * sizeof(float4) + 2 * sizeof(int) + sizeof(unsigned long long)) + (size_t)S.NH * sizeof(float4);
         LaunchScope ls(s, K_NEAR_CELL);
         const bool scalar = s->tune[KMC_TUNE_NEAR_SCALAR] == 1;
+        // blocks per cell (tuning): the item rounds of a cell spread over `split` blocks,
+        // results unchanged
+        const int split = s->tune[KMC_TUNE_NEAR_SPLIT] > 0 ? s->tune[KMC_TUNE_NEAR_SPLIT] : 1;
         const bool sil = lattice_takes_self(s);
         if (scalar && chunk == 256)
-            k_near_cell_mixed<false, 256><<<S.ncell, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil);
+            k_near_cell_mixed<false, 256><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split);
         else if (scalar)
-            k_near_cell_mixed<false, 128><<<S.ncell, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil);
+            k_near_cell_mixed<false, 128><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split);
         else if (chunk == 256)
-            k_near_cell_mixed<true, 256><<<S.ncell, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil);
+            k_near_cell_mixed<true, 256><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split);
         else
             if (S.L == 12)
-                k_near_cell_mixed<true, 128, 12><<<S.ncell, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil);
+                k_near_cell_mixed<true, 128, 12><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split);
             else
-                k_near_cell_mixed<true, 128><<<S.ncell, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil);
+                k_near_cell_mixed<true, 128><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split);
     } else {
         const size_t smem = kNearChunk * (sizeof(double4_32a) + sizeof(int)) + (size_t)S.NH * sizeof(double2);
         LaunchScope ls(s, K_NEAR_CELL);

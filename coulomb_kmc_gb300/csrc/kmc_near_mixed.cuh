@@ -261,7 +261,8 @@ constexpr int kNearMixedThreads = 32;
 // LT > 0: the expansion order is the compile-time LT (far-field loops unrolled)
 // self_in_lr: the per-proposal lattice kernel adds the moved pair's self term (pbc)
 template <bool PACKED, int CHUNK, int LT = 0>
-__global__ void __launch_bounds__(kNearMixedThreads) k_near_cell_mixed(const Sys S, Props P, const bool self_in_lr)
+__global__ void __launch_bounds__(kNearMixedThreads) k_near_cell_mixed(const Sys S, Props P, const bool self_in_lr,
+                                                                        const int split)
 {
     extern __shared__ float4 msm[];
     float4 *shi = msm;                       // [CHUNK]   (PACKED: [CHUNK / 2][4] pair quads)
@@ -272,7 +273,10 @@ __global__ void __launch_bounds__(kNearMixedThreads) k_near_cell_mixed(const Sys
     unsigned long long *skey = reinterpret_cast<unsigned long long *>(sprop + CHUNK);  // [CHUNK] position keys
     int *ulead = reinterpret_cast<int *>(skey), *uidx = ulead + CHUNK;  // after the sort: leaders, unique index
     __shared__ int nb_cell[27], nb_off[28], nb_d[27][3];
-    const int c = blockIdx.x;
+    // `split` blocks per cell: block `half` takes the item rounds r = half, half + split, ...
+    // (every item is computed exactly as with one block per cell, so the results do not
+    // depend on `split`; the cell's set-up is repeated by each of its blocks)
+    const int c = blockIdx.x / split, half = blockIdx.x - c * split;
     const int tid = threadIdx.x;
     const int n_old = S.cnt[c];
     const int p0 = P.cstart[c];
@@ -382,7 +386,7 @@ __global__ void __launch_bounds__(kNearMixedThreads) k_near_cell_mixed(const Sys
         __syncthreads();
     }
     const int nitems = n_old + nu;
-    for (int base = 0; base < nitems; base += kNearMixedThreads) {
+    for (int base = half * kNearMixedThreads; base < nitems; base += split * kNearMixedThreads) {
         const int rem = min(kNearMixedThreads, nitems - base);
         int sl = 1;
         while (sorted && sl * 2 * rem <= kNearMixedThreads) sl *= 2;
@@ -436,7 +440,7 @@ __global__ void __launch_bounds__(kNearMixedThreads) k_near_cell_mixed(const Sys
         for (int k0 = 0; k0 < total_nb; k0 += CHUNK) {
             const int kn = min(CHUNK, total_nb - k0);
             // a neighbourhood that fits one chunk is staged once for all item rounds
-            if (base == 0 || total_nb > CHUNK) {
+            if (base == half * kNearMixedThreads || total_nb > CHUNK) {
                 __syncthreads();
                 for (int k = tid; k < kn; k += blockDim.x) {
                     const int kk = k0 + k;
@@ -556,6 +560,7 @@ __global__ void __launch_bounds__(kNearMixedThreads) k_near_cell_mixed(const Sys
         __syncwarp();
         const df32 iwd = df_make(S.iw_hi, S.iw_lo);
         for (int k = tid; k < np; k += blockDim.x) {
+            if (((n_old + uidx[k]) / kNearMixedThreads) % split != half) continue;  // another block's leader
             const int p = sprop[k], lp = ulead[uidx[k]];
             const double pot = P.upot[lp];
             if (self_in_lr) {

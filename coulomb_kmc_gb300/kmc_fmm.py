@@ -214,20 +214,43 @@ class KMCFMM:
         return tuple(out)
 
     # ------------------------------------------------------------------
-    def _stage(self, name, arr_np, torch_dtype):
-        """Copy a host array into a persistent pinned -> device staging pair."""
+    def _staging_pair(self, name, n, torch_dtype):
         torch = _torch()
-        n = arr_np.size
         buf = self._staging.get(name)
         if buf is None or buf[0].numel() < n:
             h = torch.empty(max(n, 1), dtype=torch_dtype, pin_memory=True)
             d = torch.empty(max(n, 1), dtype=torch_dtype, device="cuda")
             buf = (h, d)
             self._staging[name] = buf
-        h, d = buf
-        h[:n].numpy()[:] = arr_np.reshape(-1)
+        return buf
+
+    def _stage(self, name, arr_np, torch_dtype):
+        """Copy a host array into a persistent pinned -> device staging pair; an array that
+        is the pinned buffer itself (host_buffers) goes to the device without a host copy."""
+        n = arr_np.size
+        h, d = self._staging_pair(name, n, torch_dtype)
+        if arr_np.ctypes.data != h.data_ptr():
+            h[:n].numpy()[:] = arr_np.reshape(-1)
         d[:n].copy_(h[:n], non_blocking=True)
         return d
+
+    def host_buffers(self, max_prop):
+        """Pinned host arrays for the host path of propose_with_dats: prop_positions
+        (N, 3 max_prop), prop_masks (N, max_prop), current_sites (N, 1) and
+        prop_energy_diffs (N, max_prop).  A caller that fills them in place and passes
+        them saves the copies into and out of the staging buffers (the data goes
+        between these pages and the device directly).  They stay valid while the
+        system's size and max_prop do not change."""
+        torch = _torch()
+        n, M = self.N, int(max_prop)
+        out = {}
+        for key, name, shape, dt in (("prop_positions", "ppos", (n, 3 * M), torch.float64),
+                                     ("prop_masks", "mask", (n, M), torch.int64),
+                                     ("current_sites", "sites", (n, 1), torch.int64),
+                                     ("prop_energy_diffs", "pde", (n, M), torch.float64)):
+            h, _ = self._staging_pair(name, n * shape[1], dt)
+            out[key] = h[:n * shape[1]].numpy().reshape(shape)
+        return out
 
     def propose_with_dats(self, site_max_counts, current_sites, prop_positions, prop_masks, prop_energy_diffs,
                           diff=True, prop_charges=None, sync=True):
@@ -280,7 +303,7 @@ class KMCFMM:
         out = h_pde[:n].numpy().reshape(pde.shape)
         if _is_torch(pde):
             pde.copy_(torch.from_numpy(out))
-        else:
+        elif pde.ctypes.data != h_pde.data_ptr():  # else the differences already sit in the caller's array
             pde[...] = out
 
     def error_counts(self):

@@ -249,14 +249,15 @@ int kmc_inject(kmc_system *s, int64_t n, const double *positions, const double *
 #define KMC_TUNE_P2L64 10 /* FP64 accept at L = 8, 12, 16: 0 column-pair kernel, 1 per-column kernel */
 #define KMC_TUNE_P2L64_CELLS 11 /* FP64 column-pair accept: cells per block, 2, 4 or 8 (0: 2) */
 #define KMC_TUNE_LR_THREADS 12 /* mixed pbc per-proposal lattice kernels: threads per block, 64, 128 or 256 (0: 128) */
-#define KMC_NTUNE 13
+#define KMC_TUNE_NEAR_SPLIT 13 /* mixed near field: blocks per cell, 1, 2 or 4 (0: 1), the cell's item rounds spread over them */
+#define KMC_NTUNE 14
 int kmc_set_tuning(kmc_system *s, int32_t key, int32_t value);
 int kmc_get_tuning(kmc_system *s, int32_t key, int32_t *value_out);
 /* Autotuner (no reference counterpart; the reference's OpenMP loops and block-256
  * CUDA launches are fixed): times `reps` launches of each candidate of the keys
- * whose variants give bit-identical results -- KMC_TUNE_LR_THREADS (after a
- * proposal set-up, mixed pbc) and KMC_TUNE_P2L64_CELLS (FP64 accept) -- on this
- * handle and keeps the fastest.  The state is not changed: the lattice kernels
+ * whose variants give bit-identical results -- KMC_TUNE_NEAR_SPLIT and
+ * KMC_TUNE_LR_THREADS (after a proposal set-up; mixed modes) and
+ * KMC_TUNE_P2L64_CELLS (FP64 accept) -- on this handle and keeps the fastest.  The state is not changed: the lattice kernels
  * rerun the last set-up's proposals into proposal scratch, the accept kernel runs
  * on a copy of the expansions.  chosen_out (may be NULL) receives all KMC_NTUNE
  * values.  Synchronises; allocates scratch for the call. */

@@ -1,7 +1,8 @@
 """Launch-shape tuning and size-bucket launches change no result.
 
-* Every candidate of the keys the autotuner searches (proposals per block of the
-  per-proposal lattice kernels, cells per block of the FP64 accept kernel) gives
+* Every candidate of the keys the autotuner searches (blocks per cell of the
+  mixed near field, proposals per block of the per-proposal lattice kernels,
+  cells per block of the FP64 accept kernel) gives
   the same selections, positions, energy and expansions, bit for bit, as the
   built-in choice, over a chain of device-driven KMC steps; so does whatever
   kmc_autotune picks.
@@ -24,7 +25,9 @@ pytestmark = pytest.mark.gpu
 def _run(tune=None, autotune=False, steps=12):
     hs = LatticeHopSystem(side=24, occupancy=0.25, seed=5)
     st = make_state(hs.positions(), hs.charges(), hs.extent)
-    k = KMCFMM(st.P, st.Q, st.domain, r=4, l=12, boundary_condition="pbc", max_move=1.0,
+    # R = 3: 4^3 cells of 216 sites, ~54 charges and many more proposals per cell, so the
+    # near field's cells take several rounds of items (the case blocks per cell changes)
+    k = KMCFMM(st.P, st.Q, st.domain, r=3, l=12, boundary_condition="pbc", max_move=1.0,
                precision="mixed_fp64_accept")
     k.initialise()
     d = KMCDriver(k, "lattice", 2.0, seed=31, lattice_side=hs.side, lattice_sites=hs.site_of, log_capacity=64)
@@ -59,6 +62,9 @@ def test_every_tuning_candidate_is_bit_identical():
     for val in (4, 8):
         got, _ = _run({_native.KMC_TUNE_P2L64_CELLS: val})
         _same(ref, got)
+    for val in (2, 4):
+        got, _ = _run({_native.KMC_TUNE_NEAR_SPLIT: val})
+        _same(ref, got)
 
 
 def test_autotuned_choice_is_bit_identical():
@@ -66,6 +72,7 @@ def test_autotuned_choice_is_bit_identical():
     got, chosen = _run(autotune=True)
     assert chosen[_native.KMC_TUNE_LR_THREADS] in (0, 64, 256)
     assert chosen[_native.KMC_TUNE_P2L64_CELLS] in (0, 4, 8)
+    assert chosen[_native.KMC_TUNE_NEAR_SPLIT] in (0, 2, 4)
     _same(ref, got)
 
 

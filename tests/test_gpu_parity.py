@@ -213,3 +213,23 @@ def test_lattice_hopping_chain():
         assert mg == mo
     assert_state_equal(g, o)
     g.free()
+
+
+def test_propose_with_dats_host_buffers_in_place():
+    """The library's pinned host arrays, filled in place, give the same differences as
+    ordinary numpy arrays (the copies through the staging buffers are skipped)."""
+    N, E, M = 150, 4.0, 3
+    g, o, rng, _ = pair("pbc", N=N)
+    smc = np.array([M], np.int64)
+    ppos = rng.uniform(-0.5 * E, 0.5 * E, (N, 3 * M))
+    masks = (rng.uniform(size=(N, M)) < 0.7).astype(np.int64)
+    ref = np.zeros((N, M))
+    g.propose_with_dats(smc, np.zeros((N, 1), np.int64), ppos, masks, ref)
+    hb = g.host_buffers(M)
+    hb["prop_positions"][:] = ppos
+    hb["prop_masks"][:] = masks
+    hb["current_sites"][:] = 0
+    hb["prop_energy_diffs"][:] = 0.0
+    g.propose_with_dats(smc, hb["current_sites"], hb["prop_positions"], hb["prop_masks"], hb["prop_energy_diffs"])
+    assert np.array_equal(hb["prop_energy_diffs"], ref)
+    g.free()
