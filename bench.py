@@ -380,7 +380,7 @@ def bench_precision_split(args):
     out = {}
     for Lx in args.orders:
         res = {}
-        for prec in ("mixed", "fp64"):
+        for prec in (args.precision, "fp64"):
             from coulomb_kmc_gb300 import KMCFMM
             from coulomb_kmc_gb300.dats import make_state
             from coulomb_kmc_gb300.driver import KMCDriver
@@ -397,9 +397,9 @@ def bench_precision_split(args):
                          "p99_ms": float(np.percentile(ps, 99))}
             d.free()
             k.free()
-        err = error_stats(side, r6, Lx, seed=2, nsteps=args.error_steps)
-        out[f"L{Lx}"] = {"mixed": res["mixed"], "fp64": res["fp64"],
-                         "mixed_vs_fp64": res["mixed"]["value"] / res["fp64"]["value"], "error": err}
+        err = error_stats(side, r6, Lx, seed=2, nsteps=args.error_steps, precision=args.precision)
+        out[f"L{Lx}"] = {"mixed": res[args.precision], "fp64": res["fp64"], "precision": args.precision,
+                         "mixed_vs_fp64": res[args.precision]["value"] / res["fp64"]["value"], "error": err}
         print(json.dumps({"L": Lx, **out[f"L{Lx}"]}), file=sys.stderr)
     line = {"metric": METRIC, "workload": "precision_split", "unit": UNIT,
             "config": {"workload": "pbc lattice-hop 64^3 sites, 65,536 charges (seed 2), R=6, L swept",
@@ -408,13 +408,13 @@ def bench_precision_split(args):
     print(json.dumps(line))
 
 
-def error_stats(side, r, Lx, seed, nsteps):
+def error_stats(side, r, Lx, seed, nsteps, precision="mixed"):
     """Mixed vs FP64 differences on identical states along an FP64-selected chain."""
     global R, L
     saved = (R, L)
     R, L = r, Lx
     try:
-        return mixed_error_stats(side, 0, nsteps=nsteps, seed=seed)
+        return mixed_error_stats(side, 0, nsteps=nsteps, seed=seed, precision=precision)
     finally:
         R, L = saved
 
@@ -526,7 +526,8 @@ def bench_serving(args):
     for rate in args.rates:
         reqs = poisson_requests(args.requests, rate, seed=4, n_range=(1000, args.max_n),
                                 k_range=(10, args.max_k))
-        srv = Server(precision="mixed", hbm_budget=150e9, max_active=args.max_active, n_workers=args.workers)
+        srv = Server(precision=args.precision, hbm_budget=150e9, max_active=args.max_active,
+                     n_workers=args.workers)
         st = srv.serve(reqs, realtime=True)
         st["peak_active"] = srv.peak_active
         out[str(rate)] = st
@@ -541,7 +542,7 @@ def bench_serving(args):
             "fp64_one_at_a_time_with_builds": p64 / w64,
             "mixed_vs_fp64": max(v["proposals_per_s"] for v in out.values()) / base,
             "mixed_vs_fp64_with_builds": max(v["proposals_per_s"] for v in out.values()) / (p64 / w64),
-            "per_rate": out,
+            "per_rate": out, "precision": args.precision,
             "config": {"workload": f"{args.requests} requests (seed 4), Poisson arrivals, N log-uniform in "
                                    f"[1000, {args.max_n}], lattice-hop pbc or off-lattice free_space with "
                                    f"probability 1/2, L=12, K uniform in [10, {args.max_k}], 150 GB budget",
