@@ -862,8 +862,13 @@ def bench_config4(args, rank, world, local):
     srv = Server(precision=prec, n_workers=args.workers)
     # the round's launch structure (per-system graphs on worker streams, or one graph per
     # size bucket): both timed over a few rounds (untimed warm-up rounds), the faster kept
+    # blocks per cell of the near field repeat each cell's set-up per block: tuned on whole
+    # rounds (bit-identical candidates; the rounds are untimed warm-up rounds)
+    split, split_ms = srv.autotune_key(slots, _native.KMC_TUNE_NEAR_SPLIT, (1, 2), rounds=2)
     mode, mode_ms = srv.autotune_launch(slots, rounds=3)
-    extras["autotune"] = {"kernel_launch_shapes": tuned, "round_launch": mode, "round_ms_by_launch": mode_ms}
+    extras["autotune"] = {"kernel_launch_shapes": tuned, "near_blocks_per_cell": split,
+                          "round_ms_by_near_blocks_per_cell": split_ms, "round_launch": mode,
+                          "round_ms_by_launch": mode_ms}
     if world > 1:
         import torch.distributed as dist
         dist.barrier()

@@ -767,8 +767,12 @@ int lr_cache_fill(kmc_system *s, const AcceptRec *rec = nullptr, cudaStream_t st
             return KMC_OK;
         }
         LaunchScope ls(s, rec ? K_ACCEPT_MPOLE : K_LR_OLD, st);
-        k_lr_fill64<<<gb, kLf64Warps * 32, (size_t)kLf64Warps * S.NH * sizeof(double2), st>>>(
-            S, s->d_hc, s->hc_stride, s->d_hself, rec);
+        if (rec)
+            k_lr_refresh64<<<1, kLr1Threads, S.NH * sizeof(double2) + kLr1Threads * sizeof(double), st>>>(
+                S, s->d_hc, s->hc_stride, s->d_hself, rec);
+        else
+            k_lr_fill64<<<gb, kLf64Warps * 32, (size_t)kLf64Warps * S.NH * sizeof(double2), st>>>(
+                S, s->d_hc, s->hc_stride, s->d_hself, rec);
         KMC_LAUNCH_CHECK();
         if (!rec) s->hc_valid = true;
         return KMC_OK;

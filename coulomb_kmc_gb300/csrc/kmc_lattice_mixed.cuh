@@ -362,6 +362,54 @@ __global__ void __launch_bounds__(kLf64Warps * 32) k_lr_fill64(const Sys S, floa
     if (lane == 0) hself[px] = 0.5 * S.E * bh;
 }
 
+// The accepted charge's FP64 cache entry on one block: warp 0 forms b = q a(x) (lanes
+// over the m columns) in shared memory, then every thread takes rows of A (one row per
+// thread; a 78-row form fits one pass of kLr1Threads), and b.h is summed by the block
+// in a fixed order.  The same operations per row as k_lr_fill64, whose single warp
+// walked the rows in turn.
+constexpr int kLr1Threads = 256;
+__global__ void __launch_bounds__(kLr1Threads) k_lr_refresh64(const Sys S, float2 *h32, const int hstride,
+                                                            double *hself, const AcceptRec *rec)
+{
+    extern __shared__ double2 lr1[];  // b [NH], then the rows' b.h terms [kLr1Threads]
+    if (rec->skip) return;
+    const int px = rec->pid, NH = S.NH;
+    double2 *b = lr1;
+    double *part = reinterpret_cast<double *>(b + NH);
+    if (threadIdx.x < 32)
+        multipole_warp_add(b, S.L, S.q[px], S.pos[3 * (size_t)px], S.pos[3 * (size_t)px + 1],
+                           S.pos[3 * (size_t)px + 2], true);
+    __syncthreads();
+    double bh = 0.0;
+    for (int r = threadIdx.x; r < NH; r += blockDim.x) {
+        double t0 = 0.0, t1 = 0.0, u0 = 0.0, u1 = 0.0;
+        int k = S.ar_ptr[r];
+        const int kb = S.ar_ptr[r + 1];
+        for (; k + 1 < kb; k += 2) {
+            t0 = fma(S.ar_val[k], b[S.ar_col[k]].x, t0);
+            t1 = fma(S.ar_val[k + 1], b[S.ar_col[k + 1]].x, t1);
+        }
+        if (k < kb) t0 = fma(S.ar_val[k], b[S.ar_col[k]].x, t0);
+        k = S.ai_ptr[r];
+        const int kd = S.ai_ptr[r + 1];
+        for (; k + 1 < kd; k += 2) {
+            u0 = fma(S.ai_val[k], b[S.ai_col[k]].y, u0);
+            u1 = fma(S.ai_val[k + 1], b[S.ai_col[k + 1]].y, u1);
+        }
+        if (k < kd) u0 = fma(S.ai_val[k], b[S.ai_col[k]].y, u0);
+        const double t = t0 + t1, u = u0 + u1, e = S.escale[r];
+        h32[(size_t)r * hstride + px] = make_float2((float)(t * e), (float)(u * e));
+        bh = fma(b[r].x, t, fma(b[r].y, u, bh));
+    }
+    part[threadIdx.x] = bh;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st) part[threadIdx.x] += part[threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) hself[px] = 0.5 * S.E * part[0];
+}
+
 // Fused mixed lattice term: a block takes kLfMovers moving charges (one per lane)
 // and kLfWarps warps.  (1) b = q_o a(x_o) into shared planes, columns m split over
 // the warps; (2) h = A b and the old-side constant co = b.h / 2 - b.g, rows split

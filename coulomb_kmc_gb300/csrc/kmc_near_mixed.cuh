@@ -442,9 +442,9 @@ __global__ void __launch_bounds__(kNearMixedThreads) k_near_cell_mixed(const Sys
             // a neighbourhood that fits one chunk is staged once for all item rounds
             if (base == half * kNearMixedThreads || total_nb > CHUNK) {
                 __syncthreads();
+                int j = 0;  // the neighbour cell of kk; kk only grows, so the search resumes
                 for (int k = tid; k < kn; k += blockDim.x) {
                     const int kk = k0 + k;
-                    int j = 0;
                     while (nb_off[j + 1] <= kk) ++j;
                     const size_t a = (size_t)nb_cell[j] * S.cap + (kk - nb_off[j]);
                     float4 h = S.st_hi[a];

@@ -229,6 +229,28 @@ class Server:
             s.done += 1
         return e0.elapsed_time(e1)
 
+    def autotune_key(self, slots, key, candidates, rounds=2):
+        """Tune one launch-shape key whose variants give bit-identical results on whole
+        rounds of `slots` (the device full, as in service): each candidate is set on
+        every system, the steps captured again and `rounds` rounds timed (real rounds:
+        the systems advance identically under every candidate); the fastest is kept.
+        Returns (value, {value: median round ms})."""
+        timing = {}
+
+        def apply(v):
+            for sl in slots:
+                sl.kmc.set_tuning(key, v)
+                sl.drv.capture()
+            self.free_buckets()
+
+        for v in candidates:
+            apply(v)
+            self.round(slots)
+            timing[v] = float(np.median([self.round(slots) for _ in range(rounds)]))
+        best = min(timing, key=timing.get)
+        apply(best)
+        return best, timing
+
     def autotune_launch(self, slots, rounds=3):
         """Time `rounds` rounds with each launch structure and keep the faster (the
         rounds are real rounds: every system advances, identically in either mode)."""

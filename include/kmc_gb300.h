@@ -255,9 +255,12 @@ int kmc_set_tuning(kmc_system *s, int32_t key, int32_t value);
 int kmc_get_tuning(kmc_system *s, int32_t key, int32_t *value_out);
 /* Autotuner (no reference counterpart; the reference's OpenMP loops and block-256
  * CUDA launches are fixed): times `reps` launches of each candidate of the keys
- * whose variants give bit-identical results -- KMC_TUNE_NEAR_SPLIT and
- * KMC_TUNE_LR_THREADS (after a proposal set-up; mixed modes) and
- * KMC_TUNE_P2L64_CELLS (FP64 accept) -- on this handle and keeps the fastest.  The state is not changed: the lattice kernels
+ * whose variants give bit-identical results and the same total work --
+ * KMC_TUNE_LR_THREADS (after a proposal set-up, mixed pbc) and
+ * KMC_TUNE_P2L64_CELLS (FP64 accept) -- on this handle and keeps the fastest.
+ * KMC_TUNE_NEAR_SPLIT, also bit-identical, repeats each cell's set-up per block:
+ * it is tuned on whole rounds of many systems (the Python server), where the
+ * device is full, not on one handle alone.  The state is not changed: the lattice kernels
  * rerun the last set-up's proposals into proposal scratch, the accept kernel runs
  * on a copy of the expansions.  chosen_out (may be NULL) receives all KMC_NTUNE
  * values.  Synchronises; allocates scratch for the call. */
