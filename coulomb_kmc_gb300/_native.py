@@ -54,6 +54,7 @@ KMC_DRIVE = {"lattice": 0, "offlattice": 1}
 KMC_TUNE_P2L64_CELLS = 11
 KMC_TUNE_LR_THREADS = 12
 KMC_TUNE_NEAR_SPLIT = 13
+KMC_TUNE_NEAR_OLD = 14
 
 
 def _nvcc():
@@ -177,8 +178,8 @@ class DedicatedStream:
             pass
 
 
-NKERNELS = 18
-NTUNE = 14
+NKERNELS = 19
+NTUNE = 15
 
 
 def check(rc, what):

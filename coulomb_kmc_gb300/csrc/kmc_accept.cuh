@@ -1216,3 +1216,126 @@ size_t p2l64_smem(const int L, const int NH, const int cpb, const int nsrc)
     const size_t red = (size_t)kP64Groups * cpb * NH * sizeof(double2);
     return std::max(geo, red);
 }
+
+// ---------------------------------------------------------------------------
+// The near-field potential of every charge (S.phin) across an accepted move of
+// charge k from a (cell co) to b (cell cn).  The old side of a proposal is its
+// charge times its potential, near field plus cell expansion (direct_old,
+// kmc_local.py:956-1019, recomputed on every propose there); the near-field part
+// changes only for the charges whose 27 cells hold co or cn, so it is kept per
+// charge and updated here: every other charge j loses q_k / |x_j - a'| for each of
+// its neighbour cells (with that cell's periodic shift) that is co, and gains
+// q_k / |x_j - b'| for each that is cn; k's potential at b is the sum of q_j over
+// those same distances to b (the neighbour relation is symmetric, images
+// included).  Blocks 0..26 take the cells around co, 27..53 those around cn (a
+// cell listed before is left to its first block), one thread per charge, the
+// offsets in a fixed order: each charge is updated once, the same way on every
+// run.  k's potential: a fixed-order tree per block, the blocks' partial sums
+// added in block order by the last block to finish (a ticket, no waiting).  Runs
+// after k_accept_prep (positions and the store final); nothing for a refused or
+// skipped accept.
+// ---------------------------------------------------------------------------
+constexpr int kPhinThreads = 128, kPhinBlocks = 54;
+
+// neighbour cell `o` (0..26, x fastest) of cell (cx, cy, cz) and its periodic shift;
+// false where a free-space neighbour does not exist
+__device__ __forceinline__ bool nb_cell_shift(const Sys &S, const int cx, const int cy, const int cz, const int o,
+                                              int &cell, double &sx, double &sy, double &sz)
+{
+    int c3[3] = {cx + o % 3 - 1, cy + (o / 3) % 3 - 1, cz + o / 9 - 1};
+    double sh[3] = {0.0, 0.0, 0.0};
+    for (int t = 0; t < 3; ++t) {
+        if (c3[t] < 0) {
+            if (!S.periodic) return false;
+            c3[t] += S.n;
+            sh[t] = -S.E;
+        } else if (c3[t] >= S.n) {
+            if (!S.periodic) return false;
+            c3[t] -= S.n;
+            sh[t] = S.E;
+        }
+    }
+    cell = c3[0] + S.n * (c3[1] + S.n * c3[2]);
+    sx = sh[0];
+    sy = sh[1];
+    sz = sh[2];
+    return true;
+}
+
+__global__ void __launch_bounds__(kPhinThreads) k_phin_move(const Sys S, const AcceptRec *rec, double *part,
+                                                            unsigned *ticket)
+{
+    __shared__ int cand[kPhinBlocks], nbc[27];
+    __shared__ double nbs[27][3], red[kPhinThreads];
+    __shared__ bool last;
+    if (rec->skip) return;
+    const int k = rec->pid, co = rec->co, cn = rec->cn, n = S.n;
+    const int b = blockIdx.x, t = threadIdx.x;
+    const double q = rec->q;
+    double sx, sy, sz;
+    if (t < kPhinBlocks) {
+        const int base = t < 27 ? co : cn;
+        int c;
+        cand[t] = nb_cell_shift(S, base % n, (base / n) % n, base / (n * n), t % 27, c, sx, sy, sz) ? c : -1;
+    }
+    __syncthreads();
+    const int mine = cand[b];
+    bool dup = true;
+    if (mine >= 0) dup = __syncthreads_or(t < b && cand[t] == mine);
+    double w = 0.0;  // this thread's part of k's potential at b
+    if (!dup) {
+        if (t < 27) {
+            int c;
+            nbc[t] = nb_cell_shift(S, mine % n, (mine / n) % n, mine / (n * n), t, c, sx, sy, sz) ? c : -1;
+            nbs[t][0] = sx;
+            nbs[t][1] = sy;
+            nbs[t][2] = sz;
+        }
+        __syncthreads();
+        const int cnt = S.cnt[mine];
+        for (int i = t; i < cnt; i += blockDim.x) {
+            const size_t a = (size_t)mine * S.cap + i;
+            const int j = S.store_pid[a];
+            if (j == k) continue;
+            const double4_32a v = S.store[a];
+            double d = 0.0, u = 0.0;
+            for (int o = 0; o < 27; ++o) {
+                const int nb = nbc[o];
+                if (nb == co) {
+                    const double dx = v.x - (rec->xo + nbs[o][0]), dy = v.y - (rec->yo + nbs[o][1]),
+                                 dz = v.z - (rec->zo + nbs[o][2]);
+                    d -= q * rsqrt(dx * dx + dy * dy + dz * dz);
+                }
+                if (nb == cn) {
+                    const double dx = v.x - (rec->xn + nbs[o][0]), dy = v.y - (rec->yn + nbs[o][1]),
+                                 dz = v.z - (rec->zn + nbs[o][2]);
+                    const double inv = rsqrt(dx * dx + dy * dy + dz * dz);
+                    d += q * inv;
+                    u += inv;
+                }
+            }
+            S.phin[j] += d;
+            w += v.w * u;
+        }
+    }
+    red[t] = w;
+    __syncthreads();
+    for (int h = kPhinThreads / 2; h > 0; h >>= 1) {
+        if (t < h) red[t] += red[t + h];
+        __syncthreads();
+    }
+    if (t == 0) {
+        part[b] = red[0];
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == (unsigned)gridDim.x - 1u;
+    }
+    __syncthreads();
+    if (last && t == 0) {
+        __threadfence();
+        const volatile double *vp = part;
+        double sum = 0.0;
+        for (int e = 0; e < kPhinBlocks; ++e) sum += vp[e];
+        S.phin[k] = sum;
+        *ticket = 0u;
+    }
+}

@@ -42,6 +42,8 @@ struct Sys {
     double *q;
     int *pcell;
     int *pslot;
+    double *phin;  // [N] near-field potential of each charge at its position (sum over the 27
+                   // cells around it, itself excluded), set at initialisation, kept by every accept
     double2 *lexp;
     double2 *mpole;
     // folded lattice quadratic form (pbc)

@@ -68,13 +68,16 @@ __device__ __forceinline__ f2x f2_zero_lanes(const f2x v, const bool z0, const b
     return f2_pack(z0 ? 0.0f : a, z1 ? 0.0f : b);
 }
 
-// acc(hi, lo) += t(hi) - nt(lo negated), lane-wise, in the accumulator form of
-// df_acc: two_sum on the high words, the rest gathered in the low word
-__device__ __forceinline__ void f2_acc_neg(f2x &ah, f2x &al, const f2x th, const f2x ntl)
+// both lanes negated: a flip of their sign bits (exact; integer pipe)
+__device__ __forceinline__ f2x f2_neg(const f2x v) { return v ^ 0x8000000080000000ull; }
+
+// acc(hi, lo) += t(hi) + pl(lo), lane-wise, in the accumulator form of df_acc:
+// two_sum on the high words, the rest gathered in the low word
+__device__ __forceinline__ void f2_acc(f2x &ah, f2x &al, const f2x th, const f2x pl)
 {
     const f2x s = f2_add(ah, th);
     const f2x bb = f2_sub(s, ah);
     const f2x e = f2_add(f2_sub(ah, f2_sub(s, bb)), f2_sub(th, bb));
     ah = s;
-    al = f2_add(al, f2_sub(e, ntl));
+    al = f2_add(al, f2_add(e, pl));
 }

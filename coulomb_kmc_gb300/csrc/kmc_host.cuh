@@ -27,6 +27,7 @@ struct kmc_system {
     // device buffers
     double *d_pos = nullptr, *d_q = nullptr;
     int *d_pcell = nullptr, *d_pslot = nullptr, *d_cnt = nullptr, *d_store_pid = nullptr;
+    double *d_phin = nullptr;  // Sys::phin
     double4_32a *d_store = nullptr;
     double2 *d_lexp = nullptr, *d_mpole = nullptr;
     int *d_ar_ptr = nullptr, *d_ar_col = nullptr, *d_ai_ptr = nullptr, *d_ai_col = nullptr;
@@ -40,6 +41,8 @@ struct kmc_system {
     double *d_sp_part = nullptr;    // [kSpBlocks] single-move partials
     unsigned *d_sp_ticket = nullptr;  // single-move blocks finished (reset by the last)
     unsigned *d_mg_ticket = nullptr;  // multipole / lattice-vector blocks finished
+    double *d_phin_part = nullptr;    // [kPhinBlocks] partial sums of the moved charge's near-field potential
+    unsigned *d_phin_ticket = nullptr;  // near-potential update blocks finished (reset by the last)
     unsigned long long *d_err = nullptr; // [0] bad moves, [1] overflows, [2..5] refused move (pid + 1, position bits)
     int64_t layout_gen = 0;  // advances whenever device buffers a captured step reads are reallocated
     bool props_ready = false;  // a proposal set-up has run: the compacted proposals are valid
@@ -80,12 +83,13 @@ namespace {
 // kernel ids for kmc_profile_read (order = names in kmc_kernel_name)
 enum KId { K_COUNT_SCAN = 0, K_SCAN_PART, K_SCATTER, K_OLD, K_NEW, K_LR, K_ACCEPT_PREP, K_ACCEPT_MPOLE, K_P2L,
            K_FILL, K_INIT, K_CELL_SORT, K_NEAR_CELL, K_LR_OLD, K_DIFF, K_REFRESH, K_SINGLE, K_LR_G,
-           K_NKERNELS };
+           K_PHIN, K_NKERNELS };
 const char *const g_kernel_names[K_NKERNELS] = {"count_scan", "scan_part", "scatter", "old_side", "new_side",
                                                 "far_lattice", "accept_prep", "accept_multipole",
                                                 "accept_p2l", "fill_moves", "initial_solve", "cell_sort",
                                                 "near_far_cell", "far_lattice_old", "diff", "mixed_refresh",
-                                                "single_move_fp64", "lattice_g_update"};
+                                                "single_move_fp64", "lattice_g_update",
+                                                "near_potential_update"};
 
 cudaEvent_t pool_event(kmc_system *s)
 {
@@ -521,6 +525,7 @@ void sync_sys_ptrs(kmc_system *s)
     S.q = s->d_q;
     S.pcell = s->d_pcell;
     S.pslot = s->d_pslot;
+    S.phin = s->d_phin;
     S.lexp = s->d_lexp;
     S.mpole = s->d_mpole;
     S.ar_ptr = s->d_ar_ptr;
@@ -1037,6 +1042,9 @@ int propose_evaluate(kmc_system *s, int64_t n_old_grid, int64_t n_new_grid, doub
     const Sys &S = s->S;
     int rc = lattice_fork(s, n_old_grid, n_new_grid, S.mixed != 0);
     if (rc) return rc;
+    // the moving charges' near-field potentials from S.phin unless the tuning asks for
+    // them summed afresh (the accepts keep S.phin current either way)
+    const bool kept = s->tune[KMC_TUNE_NEAR_OLD] != 1;
     if (S.mixed) {
         // 128 staged neighbours per chunk keep a one-warp block near 7 KB of shared
         // memory, so about 28 blocks fit an SM and a 4,096-cell grid runs in one wave
@@ -1050,20 +1058,20 @@ int propose_evaluate(kmc_system *s, int64_t n_old_grid, int64_t n_new_grid, doub
         const int split = s->tune[KMC_TUNE_NEAR_SPLIT] > 0 ? s->tune[KMC_TUNE_NEAR_SPLIT] : 1;
         const bool sil = lattice_takes_self(s);
         if (scalar && chunk == 256)
-            k_near_cell_mixed<false, 256><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split);
+            k_near_cell_mixed<false, 256><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split, kept);
         else if (scalar)
-            k_near_cell_mixed<false, 128><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split);
+            k_near_cell_mixed<false, 128><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split, kept);
         else if (chunk == 256)
-            k_near_cell_mixed<true, 256><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split);
+            k_near_cell_mixed<true, 256><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split, kept);
         else
             if (S.L == 12)
-                k_near_cell_mixed<true, 128, 12><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split);
+                k_near_cell_mixed<true, 128, 12><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split, kept);
             else
-                k_near_cell_mixed<true, 128><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split);
+                k_near_cell_mixed<true, 128><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split, kept);
     } else {
         const size_t smem = kNearChunk * (sizeof(double4_32a) + sizeof(int)) + (size_t)S.NH * sizeof(double2);
         LaunchScope ls(s, K_NEAR_CELL);
-        k_near_cell<<<S.ncell, kNearThreads, smem, s->stream>>>(S, s->P);
+        k_near_cell<<<S.ncell, kNearThreads, smem, s->stream>>>(S, s->P, kept);
     }
     KMC_LAUNCH_CHECK();
     return run_finish(s, n_new_grid, out);

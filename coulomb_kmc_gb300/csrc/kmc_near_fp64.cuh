@@ -48,7 +48,9 @@ __device__ __forceinline__ double far_eval_shared(const double2 *Lc, const int L
 constexpr int kNearThreads = 64;
 constexpr int kNearChunk = 256;
 
-__global__ void __launch_bounds__(kNearThreads) k_near_cell(const Sys S, Props P)
+// kept: the moving charges' near-field potentials are taken from S.phin (kept by
+// every accept), so they only evaluate the cell expansion
+__global__ void __launch_bounds__(kNearThreads) k_near_cell(const Sys S, Props P, const bool kept)
 {
     extern __shared__ double4_32a nsm[];
     double4_32a *stg = nsm;                                    // [kNearChunk]
@@ -88,14 +90,23 @@ __global__ void __launch_bounds__(kNearThreads) k_near_cell(const Sys S, Props P
     __syncthreads();
     const int total_nb = nb_off[27];
     const double ccx = cell_centre(S, cx), ccy = cell_centre(S, cy), ccz = cell_centre(S, cz);
-    const int nitems = n_old + np;
+    const int n_po = kept ? 0 : n_old;  // moving charges among the pair loop's items
+    if (kept)
+        for (int o = tid; o < n_old; o += blockDim.x) {
+            const int pidx = S.store_pid[(size_t)c * S.cap + o];
+            if (P.cnt[pidx] <= 0) continue;
+            const double x = S.pos[3 * (size_t)pidx], y = S.pos[3 * (size_t)pidx + 1], z = S.pos[3 * (size_t)pidx + 2];
+            const double q = S.q[pidx];
+            P.u0p[pidx] = q * S.phin[pidx] + q * far_eval_shared(lc, S.L, x - ccx, y - ccy, z - ccz);
+        }
+    const int nitems = n_po + np;
     for (int base = 0; base < nitems; base += blockDim.x) {
         const int item = base + tid;
         bool act = item < nitems;
         double x = 0.0, y = 0.0, z = 0.0, q = 0.0;
         int self = -1, pidx = -1, p = -1;
         if (act) {
-            if (item < n_old) {
+            if (item < n_po) {
                 pidx = S.store_pid[(size_t)c * S.cap + item];
                 act = P.cnt[pidx] > 0;  // only charges with proposals need their old-side energy
                 self = pidx;
@@ -104,7 +115,7 @@ __global__ void __launch_bounds__(kNearThreads) k_near_cell(const Sys S, Props P
                 z = S.pos[3 * (size_t)pidx + 2];
                 q = S.q[pidx];
             } else {
-                p = P.cprops[p0 + item - n_old];
+                p = P.cprops[p0 + item - n_po];
                 x = P.ppos[3 * (size_t)p];
                 y = P.ppos[3 * (size_t)p + 1];
                 z = P.ppos[3 * (size_t)p + 2];

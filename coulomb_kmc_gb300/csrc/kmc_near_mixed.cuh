@@ -120,73 +120,70 @@ __device__ __forceinline__ df32 far_eval_mixed(const float4 *Lc, const int Lr, c
 
 // q_j / r for an item (grid coordinates ph + pl, cell widths) and a staged
 // neighbour (h = grid high words and q_hi, l = low words and q_lo):
-//   s = ph - h and S = |s|^2 exact (grid_split);
-//   r2l = 2 s.l + |l|^2 in FP32 (relative error of r^2 about 2^-24 |r2l| / r^2,
-//   ~2^-30 at the nearest lattice distance, 2^-24 for charges within 2^-10 cell
-//   widths of each other);
+//   s = ph - h and S = |s|^2 exact (grid_split: 12-bit high words);
+//   r2l = 2 s.l + |l|^2 = l.(2 s + l) in FP32 (relative error of r^2 about
+//   2^-24 |r2l| / r^2, ~2^-30 at the nearest lattice distance, 2^-24 for charges
+//   within 2^-10 cell widths of each other);
 //   r^2 = r2h + r2e exactly (fast two-sum, S >= |r2l| unless the pair is that close);
-//   1/r = y + y/2 (1 - r^2 y^2) with y = rsqrtf(r2h), the residual formed with FMA
-//   (df_rsqrt); the charge product error-free.
-// Returns th and the negated low word nte (q_j / r = th - nte).  near_pair_g and
-// its packed form near_pair_g2 perform the same roundings in the same order.
+//   1/r = y + y/2 (1 - r^2 y^2) with y = rsqrtf(r2h), the residual r^2 y^2 - 1
+//   formed with FMA from the exact square y^2 = yy + e (Newton's step for the
+//   inverse square root, its error ~3/8 (1 - r^2 y^2)^2 ~ 2^-44);
+//   the charge product error-free, the Newton term as q_hi y ~ th (2^-24 relative
+//   of a 2^-22 correction).
+// Returns th and the low part pl (q_j / r = th + pl).  near_pair_g and its packed
+// form near_pair_g2 perform the same roundings in the same order.
 struct NearPoint {
     float xh, xl, yh, yl, zh, zl;
 };
 
-__device__ __forceinline__ void near_pair_g(const NearPoint &p, const float4 h, const float4 l, float &th, float &nte)
+__device__ __forceinline__ void near_pair_g(const NearPoint &p, const float4 h, const float4 l, float &th, float &pl)
 {
     const float sx = p.xh - h.x, sy = p.yh - h.y, sz = p.zh - h.z;
     const float lx = p.xl - l.x, ly = p.yl - l.y, lz = p.zl - l.z;
     const float S2 = fmaf(sx, sx, fmaf(sy, sy, sz * sz));
-    const float dt = fmaf(sx, lx, fmaf(sy, ly, sz * lz));
-    const float ll = fmaf(lx, lx, fmaf(ly, ly, lz * lz));
-    const float r2l = fmaf(2.0f, dt, ll);
+    const float ux = fmaf(2.0f, sx, lx), uy = fmaf(2.0f, sy, ly), uz = fmaf(2.0f, sz, lz);
+    const float r2l = fmaf(lx, ux, fmaf(ly, uy, lz * uz));
     const float r2h = S2 + r2l;
-    const float nr2e = (r2h - S2) - r2l;
+    const float r2e = r2l - (r2h - S2);
     const float y = rsqrtf(r2h);
     const float yy = y * y;
-    const float nyye = fmaf(-y, y, yy);
-    const float a1 = fmaf(-r2h, yy, 1.0f);
-    const float rho = fmaf(r2h, nyye, fmaf(nr2e, yy, a1));
-    const float nrlo = (-0.5f * y) * rho;
+    const float e = fmaf(y, y, -yy);
+    const float a1 = fmaf(r2h, yy, -1.0f);
+    const float nrho = fmaf(r2h, e, fmaf(r2e, yy, a1));  // r^2 y^2 - 1
     th = h.w * y;
-    nte = fmaf(h.w, -y, th);
-    nte = fmaf(l.w, -y, nte);
-    nte = fmaf(h.w, nrlo, nte);
+    pl = fmaf(h.w, y, -th);
+    pl = fmaf(l.w, y, pl);
+    pl = fmaf(-0.5f * th, nrho, pl);
 }
 
 // Packed form for two neighbours at once, lane i of each f2x holding neighbour
 // i; the staged pair is four quads a = (x_hi, y_hi), b = (z_hi, q_hi),
-// c = (x_lo, y_lo), d = (z_lo, q_lo).  Negations the packed instructions cannot
-// fold are explicit subtractions from zero (exact).
+// c = (x_lo, y_lo), d = (z_lo, q_lo).  Negations are sign-bit flips (exact, on
+// the integer pipe).
 struct NearPoint2 {
     f2x xh, xl, yh, yl, zh, zl;
-    f2x zero, one, two, half;  // packed constants, kept in registers across the pair loop
+    f2x mone, two, mhalf;  // packed constants -1, 2, -1/2, kept in registers across the pair loop
 };
 
 __device__ __forceinline__ void near_pair_g2(const NearPoint2 &p, const ulonglong2 a, const ulonglong2 b,
-                                             const ulonglong2 c, const ulonglong2 d, f2x &th, f2x &ntl)
+                                             const ulonglong2 c, const ulonglong2 d, f2x &th, f2x &pl)
 {
     const f2x sx = f2_sub(p.xh, a.x), sy = f2_sub(p.yh, a.y), sz = f2_sub(p.zh, b.x);
     const f2x lx = f2_sub(p.xl, c.x), ly = f2_sub(p.yl, c.y), lz = f2_sub(p.zl, d.x);
     const f2x S2 = f2_fma(sx, sx, f2_fma(sy, sy, f2_mul(sz, sz)));
-    const f2x dt = f2_fma(sx, lx, f2_fma(sy, ly, f2_mul(sz, lz)));
-    const f2x ll = f2_fma(lx, lx, f2_fma(ly, ly, f2_mul(lz, lz)));
-    const f2x zero = p.zero;
-    const f2x r2l = f2_fma(p.two, dt, ll);
+    const f2x ux = f2_fma(p.two, sx, lx), uy = f2_fma(p.two, sy, ly), uz = f2_fma(p.two, sz, lz);
+    const f2x r2l = f2_fma(lx, ux, f2_fma(ly, uy, f2_mul(lz, uz)));
     const f2x r2h = f2_add(S2, r2l);
-    const f2x nr2e = f2_sub(f2_sub(r2h, S2), r2l);
+    const f2x r2e = f2_sub(r2l, f2_sub(r2h, S2));
     const f2x y = f2_rsqrt(r2h);
     const f2x yy = f2_mul(y, y);
-    const f2x ny = f2_sub(zero, y);
-    const f2x nyye = f2_fma(ny, y, yy);
-    const f2x a1 = f2_fma(f2_sub(zero, r2h), yy, p.one);
-    const f2x rho = f2_fma(r2h, nyye, f2_fma(nr2e, yy, a1));
-    const f2x nrlo = f2_mul(f2_mul(p.half, ny), rho);
+    const f2x e = f2_fma(y, y, f2_neg(yy));
+    const f2x a1 = f2_fma(r2h, yy, p.mone);
+    const f2x nrho = f2_fma(r2h, e, f2_fma(r2e, yy, a1));
     th = f2_mul(b.y, y);
-    ntl = f2_fma(b.y, ny, th);
-    ntl = f2_fma(d.y, ny, ntl);
-    ntl = f2_fma(b.y, nrlo, ntl);
+    pl = f2_fma(b.y, y, f2_neg(th));
+    pl = f2_fma(d.y, y, pl);
+    pl = f2_fma(f2_mul(p.mhalf, th), nrho, pl);
 }
 
 // The 26 periodic images of the moved-pair self term other than the nearest (ks, in
@@ -239,9 +236,9 @@ __device__ __forceinline__ df32 self_term_grid(const Sys &S, const int cx, const
         for (int t = 0; t < 3; ++t) k[t] = max(-1, min(1, (int)(-rintf(sh[t] / (float)n))));
     const NearPoint dp{sh[0] + (float)(k[0] * n), sl[0], sh[1] + (float)(k[1] * n), sl[1],
                        sh[2] + (float)(k[2] * n), sl[2]};
-    float th, nte;
-    near_pair_g(dp, make_float4(0.f, 0.f, 0.f, 1.f), make_float4(0.f, 0.f, 0.f, 0.f), th, nte);
-    df32 e = df_make(th, -nte);
+    float th, pl;
+    near_pair_g(dp, make_float4(0.f, 0.f, 0.f, 1.f), make_float4(0.f, 0.f, 0.f, 0.f), th, pl);
+    df32 e = df_make(th, pl);
     if (!S.periodic) return e;
     const int m2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
     if (m2) e = df_sub(e, df_rsqrt(df_make((float)(m2 * n * n), 0.f)));
@@ -260,9 +257,12 @@ constexpr int kNearMixedThreads = 32;
 // FP32 instructions (near_pair_g2); otherwise one at a time (near_pair_g).
 // LT > 0: the expansion order is the compile-time LT (far-field loops unrolled)
 // self_in_lr: the per-proposal lattice kernel adds the moved pair's self term (pbc)
+// kept: the moving charges' near-field potentials are taken from S.phin (kept by every
+// accept), so they only evaluate the cell expansion; otherwise they are items of the
+// pair loop like the proposals
 template <bool PACKED, int CHUNK, int LT = 0>
 __global__ void __launch_bounds__(kNearMixedThreads) k_near_cell_mixed(const Sys S, Props P, const bool self_in_lr,
-                                                                        const int split)
+                                                                        const int split, const bool kept)
 {
     extern __shared__ float4 msm[];
     float4 *shi = msm;                       // [CHUNK]   (PACKED: [CHUNK / 2][4] pair quads)
@@ -385,7 +385,20 @@ __global__ void __launch_bounds__(kNearMixedThreads) k_near_cell_mixed(const Sys
         nu = before;
         __syncthreads();
     }
-    const int nitems = n_old + nu;
+    const int n_po = kept ? 0 : n_old;  // moving charges among the pair loop's items
+    if (kept) {
+        const df32 wd = df_make(S.w_hi, S.w_lo);
+        for (int o = half * kNearMixedThreads + tid; o < n_old; o += split * kNearMixedThreads) {
+            const size_t a = (size_t)c * S.cap + o;
+            const int pidx = S.store_pid[a];
+            if (P.cnt[pidx] <= 0) continue;
+            const float4 gh = S.st_hi[a], gl = S.st_lo[a];
+            const df32 ff = far_eval_mixed<LT>(lc, S.L, df_mul(df_make(gh.x, gl.x), wd),
+                                               df_mul(df_make(gh.y, gl.y), wd), df_mul(df_make(gh.z, gl.z), wd));
+            P.u0p[pidx] = S.q[pidx] * (S.phin[pidx] + df_to_double(ff));
+        }
+    }
+    const int nitems = n_po + nu;
     for (int base = half * kNearMixedThreads; base < nitems; base += split * kNearMixedThreads) {
         const int rem = min(kNearMixedThreads, nitems - base);
         int sl = 1;
@@ -398,7 +411,7 @@ __global__ void __launch_bounds__(kNearMixedThreads) k_near_cell_mixed(const Sys
         if (act) {
             // the item's grid copy relative to this cell: the store's for a moving
             // charge, split here for a proposal
-            if (item < n_old) {
+            if (item < n_po) {
                 const size_t a = (size_t)c * S.cap + item;
                 pidx = S.store_pid[a];
                 act = P.cnt[pidx] > 0;
@@ -407,7 +420,7 @@ __global__ void __launch_bounds__(kNearMixedThreads) k_near_cell_mixed(const Sys
                 gl = S.st_lo[a];
                 q = S.q[pidx];
             } else {
-                p = sorted ? ulead[item - n_old] : P.cprops[p0 + item - n_old];
+                p = sorted ? ulead[item - n_po] : P.cprops[p0 + item - n_po];
                 const float2 ux = grid_split((P.ppos[3 * (size_t)p] - cell_centre(S, cx)) * S.inv_w);
                 const float2 uy = grid_split((P.ppos[3 * (size_t)p + 1] - cell_centre(S, cy)) * S.inv_w);
                 const float2 uz = grid_split((P.ppos[3 * (size_t)p + 2] - cell_centre(S, cz)) * S.inv_w);
@@ -432,10 +445,9 @@ __global__ void __launch_bounds__(kNearMixedThreads) k_near_cell_mixed(const Sys
             pp.yl = f2_splat(gy.y);
             pp.zh = f2_splat(gz.x);
             pp.zl = f2_splat(gz.y);
-            pp.zero = f2_splat(0.0f);
-            pp.one = f2_splat(1.0f);
+            pp.mone = f2_splat(-1.0f);
             pp.two = f2_splat(2.0f);
-            pp.half = f2_splat(0.5f);
+            pp.mhalf = f2_splat(-0.5f);
         }
         for (int k0 = 0; k0 < total_nb; k0 += CHUNK) {
             const int kn = min(CHUNK, total_nb - k0);
@@ -479,27 +491,27 @@ __global__ void __launch_bounds__(kNearMixedThreads) k_near_cell_mixed(const Sys
                 // pairs holding charges of this cell (staged first): with the exclusion check
                 const int jo = (max(0, min(kn, n_old - k0)) + 1) >> 1;
                 for (int j = sub; j < jo; j += sl) {
-                    f2x th0, nt0;
-                    near_pair_g2(pp, q4[4 * j], q4[4 * j + 1], q4[4 * j + 2], q4[4 * j + 3], th0, nt0);
+                    f2x th0, pl0;
+                    near_pair_g2(pp, q4[4 * j], q4[4 * j + 1], q4[4 * j + 2], q4[4 * j + 3], th0, pl0);
                     const int2 i0 = pid2[j];
                     th0 = f2_zero_lanes(th0, i0.x == self, i0.y == self);
-                    nt0 = f2_zero_lanes(nt0, i0.x == self, i0.y == self);
-                    f2_acc_neg(a0h, a0l, th0, nt0);
+                    pl0 = f2_zero_lanes(pl0, i0.x == self, i0.y == self);
+                    f2_acc(a0h, a0l, th0, pl0);
                 }
                 // the other cells' pairs: two per iteration, independent accumulators
                 int j = jo + (((sub - jo) % sl) + sl) % sl;
                 for (; j + sl < npair; j += 2 * sl) {
-                    f2x th0, nt0, th1, nt1;
-                    near_pair_g2(pp, q4[4 * j], q4[4 * j + 1], q4[4 * j + 2], q4[4 * j + 3], th0, nt0);
+                    f2x th0, pl0, th1, pl1;
+                    near_pair_g2(pp, q4[4 * j], q4[4 * j + 1], q4[4 * j + 2], q4[4 * j + 3], th0, pl0);
                     near_pair_g2(pp, q4[4 * (j + sl)], q4[4 * (j + sl) + 1], q4[4 * (j + sl) + 2],
-                                 q4[4 * (j + sl) + 3], th1, nt1);
-                    f2_acc_neg(a0h, a0l, th0, nt0);
-                    f2_acc_neg(a1h, a1l, th1, nt1);
+                                 q4[4 * (j + sl) + 3], th1, pl1);
+                    f2_acc(a0h, a0l, th0, pl0);
+                    f2_acc(a1h, a1l, th1, pl1);
                 }
                 if (j < npair) {
-                    f2x th0, nt0;
-                    near_pair_g2(pp, q4[4 * j], q4[4 * j + 1], q4[4 * j + 2], q4[4 * j + 3], th0, nt0);
-                    f2_acc_neg(a0h, a0l, th0, nt0);
+                    f2x th0, pl0;
+                    near_pair_g2(pp, q4[4 * j], q4[4 * j + 1], q4[4 * j + 2], q4[4 * j + 3], th0, pl0);
+                    f2_acc(a0h, a0l, th0, pl0);
                 }
             } else if (act) {
                 // two neighbours per iteration, independent accumulators (more ILP per warp)
@@ -508,18 +520,18 @@ __global__ void __launch_bounds__(kNearMixedThreads) k_near_cell_mixed(const Sys
                     float h0, e0, h1, e1;
                     near_pair_g(gp, shi[k], slo[k], h0, e0);
                     near_pair_g(gp, shi[k + sl], slo[k + sl], h1, e1);
-                    if (spid[k] != self) df_acc(acc, df_make(h0, -e0));
-                    if (spid[k + sl] != self) df_acc(acc1, df_make(h1, -e1));
+                    if (spid[k] != self) df_acc(acc, df_make(h0, e0));
+                    if (spid[k + sl] != self) df_acc(acc1, df_make(h1, e1));
                 }
                 if (k < kn && spid[k] != self) {
                     float h0, e0;
                     near_pair_g(gp, shi[k], slo[k], h0, e0);
-                    df_acc(acc, df_make(h0, -e0));
+                    df_acc(acc, df_make(h0, e0));
                 }
             }
         }
         if constexpr (PACKED) {
-            // four lane sums (two accumulators x two lanes), low words negated
+            // four lane sums (two accumulators x two lanes)
             float h0, h1, h2, h3, l0, l1, l2, l3;
             f2_unpack(a0h, h0, h1);
             f2_unpack(a1h, h2, h3);
@@ -560,7 +572,7 @@ __global__ void __launch_bounds__(kNearMixedThreads) k_near_cell_mixed(const Sys
         __syncwarp();
         const df32 iwd = df_make(S.iw_hi, S.iw_lo);
         for (int k = tid; k < np; k += blockDim.x) {
-            if (((n_old + uidx[k]) / kNearMixedThreads) % split != half) continue;  // another block's leader
+            if (((n_po + uidx[k]) / kNearMixedThreads) % split != half) continue;  // another block's leader
             const int p = sprop[k], lp = ulead[uidx[k]];
             const double pot = P.upot[lp];
             if (self_in_lr) {

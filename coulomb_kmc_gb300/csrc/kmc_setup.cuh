@@ -159,7 +159,8 @@ __global__ void k_fill_moves(const Sys S, Props P, const int nump)
 
 
 // ---------------------------------------------------------------------------
-// old side: U0 = q (near excluding self + far) per moving charge
+// old side: U0 = q (near excluding self + far) per moving charge; with `all`
+// (initialisation), every charge, and its near-field potential is kept in S.phin
 // ---------------------------------------------------------------------------
 __global__ void k_old(const Sys S, Props P, const int all)
 {
@@ -173,6 +174,7 @@ __global__ void k_old(const Sys S, Props P, const int all)
     const double nf = near_sum_fp64<true>(S, x, y, z, cx, cy, cz, px);
     const double ff = far_at(S, cell, x, y, z);
     P.u0p[px] = S.q[px] * nf + S.q[px] * ff;
+    if (all) S.phin[px] = nf;  // the near-field potential kept between moves
 }
 
 // self / moved-pair term  kmc_fmm_self_interaction.py:163-242

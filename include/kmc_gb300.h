@@ -191,7 +191,7 @@ int kmc_info(kmc_system *s, int64_t *ncell, int64_t *capacity, int64_t *n);
  * milliseconds and launch counts since the last reset, and the number of kernel
  * launches issued by this handle.  Counterpart of the reference's per-component
  * timers in the PROFILE dictionary (common.py:136-160, kmc_fmm.py:894-912). */
-#define KMC_NKERNELS 18
+#define KMC_NKERNELS 19
 int kmc_profile(kmc_system *s, int32_t enable);
 int kmc_profile_read(kmc_system *s, int32_t reset, double *ms_out, int64_t *count_out, int64_t *launches_out);
 /* Diagnostics, no reference counterpart: the launches bracketed since the last
@@ -250,7 +250,9 @@ int kmc_inject(kmc_system *s, int64_t n, const double *positions, const double *
 #define KMC_TUNE_P2L64_CELLS 11 /* FP64 column-pair accept: cells per block, 2, 4 or 8 (0: 2) */
 #define KMC_TUNE_LR_THREADS 12 /* mixed pbc per-proposal lattice kernels: threads per block, 64, 128 or 256 (0: 128) */
 #define KMC_TUNE_NEAR_SPLIT 13 /* mixed near field: blocks per cell, 1, 2 or 4 (0: 1), the cell's item rounds spread over them */
-#define KMC_NTUNE 14
+#define KMC_TUNE_NEAR_OLD 14 /* old side of a propose: 0 each charge's near-field potential kept between moves (every
+                                accept updates the charges around the moved one), 1 summed afresh on every propose */
+#define KMC_NTUNE 15
 int kmc_set_tuning(kmc_system *s, int32_t key, int32_t value);
 int kmc_get_tuning(kmc_system *s, int32_t key, int32_t *value_out);
 /* Autotuner (no reference counterpart; the reference's OpenMP loops and block-256
