@@ -865,10 +865,14 @@ def bench_config4(args, rank, world, local):
     # blocks per cell of the near field repeat each cell's set-up per block: tuned on whole
     # rounds (bit-identical candidates; the rounds are untimed warm-up rounds)
     split, split_ms = srv.autotune_key(slots, _native.KMC_TUNE_NEAR_SPLIT, (1, 2), rounds=2)
+    # so is the residency of the FP64 accept kernel (blocks per SM, 0 = no limit), which
+    # decides how much of each SM the other systems' near-field kernels find free
+    per_sm, per_sm_ms = srv.autotune_key(slots, _native.KMC_TUNE_P2L64_PER_SM, (0, 1, 2), rounds=2)
     mode, mode_ms = srv.autotune_launch(slots, rounds=3)
     extras["autotune"] = {"kernel_launch_shapes": tuned, "near_blocks_per_cell": split,
-                          "round_ms_by_near_blocks_per_cell": split_ms, "round_launch": mode,
-                          "round_ms_by_launch": mode_ms}
+                          "round_ms_by_near_blocks_per_cell": split_ms,
+                          "fp64_accept_blocks_per_sm": per_sm, "round_ms_by_fp64_accept_blocks_per_sm": per_sm_ms,
+                          "round_launch": mode, "round_ms_by_launch": mode_ms}
     if world > 1:
         import torch.distributed as dist
         dist.barrier()

@@ -55,6 +55,7 @@ KMC_TUNE_P2L64_CELLS = 11
 KMC_TUNE_LR_THREADS = 12
 KMC_TUNE_NEAR_SPLIT = 13
 KMC_TUNE_NEAR_OLD = 14
+KMC_TUNE_P2L64_PER_SM = 15
 
 
 def _nvcc():
@@ -179,7 +180,7 @@ class DedicatedStream:
 
 
 NKERNELS = 19
-NTUNE = 15
+NTUNE = 16
 
 
 def check(rc, what):

@@ -1210,10 +1210,10 @@ __global__ void __launch_bounds__(kP64Groups * (LT <= 12 ? 8 : 4) * (LT / 2)) k_
 
 // shared memory of k_p2l64: the geometry of every (source, cell) item, then the
 // groups' sums (the same area)
-size_t p2l64_smem(const int L, const int NH, const int cpb, const int nsrc)
+size_t p2l64_smem(const int L, const int NH, const int cpb, const int nsrc, const int G)
 {
     const size_t geo = (size_t)nsrc * cpb * (L + 1) * sizeof(double2);
-    const size_t red = (size_t)kP64Groups * cpb * NH * sizeof(double2);
+    const size_t red = (size_t)G * cpb * NH * sizeof(double2);
     return std::max(geo, red);
 }
 

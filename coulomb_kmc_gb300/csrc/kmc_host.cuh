@@ -7,6 +7,7 @@
 struct kmc_system {
     kmc_params prm{};
     int tune[KMC_NTUNE] = {};
+    int smem_sm = 0;  // shared memory per SM of the device (bytes)
     cudaStream_t stream = nullptr;
     // side stream of the accept: the move's energy and the multipole / lattice vector
     // updates run there beside the particle-to-local kernel (fork / join events)
@@ -618,14 +619,30 @@ int launch_p2l(kmc_system *s, int mode, int nsrc, const Sys *src = nullptr)
         LaunchScope ls(s, K_P2L);
         k_p2l_df<<<grd, blk, need_df(cp, G), s->stream>>>(S, s->d_rec, nsrc);
     } else if (mode == 0 && (S.L == 8 || S.L == 12 || S.L == 16) && s->tune[KMC_TUNE_P2L64] != 1 &&
-               p2l64_smem(S.L, S.NH, 1, nsrc) <= 200 * 1024) {
-        // FP64 column pairs: cpb cells x 16 source groups, a warp per pair over 2 cells; the
-        // groups (and so every rounding) do not depend on the cells per block (tuning)
+               p2l64_smem(S.L, S.NH, 1, nsrc, kP64Groups) <= 200 * 1024) {
+        // FP64 column pairs: cells x source groups x pairs, a warp per pair; the groups (and
+        // so every rounding) depend only on the number of sources: 16, or as many as the
+        // sources rounded up to a power of two when fewer (free space: the old and new
+        // position, 2 groups); the cells per block (tuning: 2, 4, 8 at 16 groups, scaled up
+        // with fewer groups to the same threads per block) change nothing in the results
+        int G = kP64Groups;
+        while (G > 1 && G / 2 >= nsrc) G /= 2;
         int cpb = s->tune[KMC_TUNE_P2L64_CELLS] > 0 ? s->tune[KMC_TUNE_P2L64_CELLS] : 2;
-        while (cpb > 2 && (p2l64_smem(S.L, S.NH, cpb, nsrc) > 200 * 1024 || (S.L > 12 && cpb > 4))) cpb /= 2;
-        dim3 blk(cpb, kP64Groups, S.L / 2);
+        cpb *= kP64Groups / G;
+        const int cmin = 2 * kP64Groups / G;
+        while (cpb > cmin && (p2l64_smem(S.L, S.NH, cpb, nsrc, G) > 200 * 1024 || (S.L > 12 && cpb * G > 4 * kP64Groups)))
+            cpb /= 2;
+        dim3 blk(cpb, G, S.L / 2);
         dim3 grd((S.ncell + cpb - 1) / cpb);
-        const size_t sm = p2l64_smem(S.L, S.NH, cpb, nsrc);
+        size_t sm = p2l64_smem(S.L, S.NH, cpb, nsrc, G);
+        // at most `per_sm` blocks resident per SM (tuning): the block's shared memory padded so
+        // that one more does not fit, which leaves the rest of each SM to the other systems'
+        // kernels (the near field) in a batch
+        const int per_sm = s->tune[KMC_TUNE_P2L64_PER_SM];
+        if (per_sm > 0 && s->smem_sm > 0) {
+            const size_t pad = (size_t)s->smem_sm / (per_sm + 1) - 1024 + 256;
+            if (pad > sm && pad <= 200 * 1024) sm = pad;
+        }
         LaunchScope ls(s, K_P2L);
         if (S.L == 8)
             k_p2l64<8><<<grd, blk, sm, s->stream>>>(S, s->d_rec, nsrc);

@@ -252,7 +252,9 @@ int kmc_inject(kmc_system *s, int64_t n, const double *positions, const double *
 #define KMC_TUNE_NEAR_SPLIT 13 /* mixed near field: blocks per cell, 1, 2 or 4 (0: 1), the cell's item rounds spread over them */
 #define KMC_TUNE_NEAR_OLD 14 /* old side of a propose: 0 each charge's near-field potential kept between moves (every
                                 accept updates the charges around the moved one), 1 summed afresh on every propose */
-#define KMC_NTUNE 15
+#define KMC_TUNE_P2L64_PER_SM 15 /* FP64 column-pair accept: at most 1..4 blocks resident per SM (0: no limit), the rest of
+                                    each SM left to other kernels; results unchanged */
+#define KMC_NTUNE 16
 int kmc_set_tuning(kmc_system *s, int32_t key, int32_t value);
 int kmc_get_tuning(kmc_system *s, int32_t key, int32_t *value_out);
 /* Autotuner (no reference counterpart; the reference's OpenMP loops and block-256

@@ -1,8 +1,9 @@
 """Launch-shape tuning and size-bucket launches change no result.
 
-* Every candidate of the keys the autotuner searches (blocks per cell of the
+* Every candidate of the keys the autotuners search (blocks per cell of the
   mixed near field, proposals per block of the per-proposal lattice kernels,
-  cells per block of the FP64 accept kernel) gives
+  cells per block and blocks per SM of the FP64 accept kernel, with 16 source
+  groups for pbc and 2 for free space) gives
   the same selections, positions, energy and expansions, bit for bit, as the
   built-in choice, over a chain of device-driven KMC steps; so does whatever
   kmc_autotune picks.
@@ -45,6 +46,26 @@ def _run(tune=None, autotune=False, steps=12):
     return out, chosen
 
 
+def _run_free(tune=None, steps=12):
+    rng = np.random.default_rng(8)
+    N, E = 3000, 22.0
+    P = rng.uniform(-0.5 * E, 0.5 * E, (N, 3))
+    Q = np.where(np.arange(N) % 2 == 0, 1.0, -1.0)
+    st = make_state(P, Q, E)
+    k = KMCFMM(st.P, st.Q, st.domain, r=4, l=12, boundary_condition="free_space", max_move=1.0,
+               precision="mixed_fp64_accept")
+    k.initialise()
+    d = KMCDriver(k, "offlattice", 1.0, seed=12, step=0.5, log_capacity=64)
+    for key, val in (tune or {}).items():
+        k.set_tuning(key, val)
+    d.capture()
+    d.launch(steps)
+    out = (d.log(), k.energy, k.state())
+    d.free()
+    k.free()
+    return out, None
+
+
 def _same(a, b):
     (la, ea, sa), (lb, eb, sb) = a, b
     for x, y in zip(la, lb):
@@ -64,6 +85,17 @@ def test_every_tuning_candidate_is_bit_identical():
         _same(ref, got)
     for val in (2, 4):
         got, _ = _run({_native.KMC_TUNE_NEAR_SPLIT: val})
+        _same(ref, got)
+    for val in (1, 2):
+        got, _ = _run({_native.KMC_TUNE_P2L64_PER_SM: val})
+        _same(ref, got)
+
+
+def test_fp64_accept_shapes_bit_identical_in_free_space():
+    ref, _ = _run_free()
+    for tune in ({_native.KMC_TUNE_P2L64_CELLS: 4}, {_native.KMC_TUNE_P2L64_CELLS: 8},
+                 {_native.KMC_TUNE_P2L64_PER_SM: 1}):
+        got, _ = _run_free(tune)
         _same(ref, got)
 
 
