@@ -629,16 +629,27 @@ def offlattice_proposals(pos, E, rng, out=None):
 
 class HostRound:
     """One Metropolis round of every system through the reference-facing API with host
-    (numpy) buffers: proposals generated on the host, propose_with_dats (host -> device
-    copies of the proposals, device -> host copy of the differences), Metropolis on the
-    host, accept.  Buffers per system are allocated once."""
+    (numpy) buffers, as a caller serving many systems would run it: worker threads,
+    each with its own CUDA stream and random generator, take the systems in turn;
+    per system, proposals generated on the host into the library's pinned arrays,
+    propose_with_dats (host -> device copies of the proposals, device -> host copy
+    of the differences; it returns when they are on the host), Metropolis on the
+    host, accept.  The library calls and numpy's bulk work release the GIL, so the
+    systems' host work and device work overlap across workers.  Buffers per system
+    are allocated once."""
 
-    def __init__(self, kmcs, seed=7):
+    def __init__(self, kmcs, seed=7, workers=16):
+        import torch
+        from concurrent.futures import ThreadPoolExecutor
+        from coulomb_kmc_gb300._native import DedicatedStream
         self.kmcs = kmcs
-        self.rng = np.random.default_rng(seed)
+        self.workers = max(1, min(workers, len(kmcs)))
+        self.rngs = [np.random.default_rng(sq) for sq in np.random.SeedSequence(seed).spawn(self.workers)]
+        self.streams = [DedicatedStream() for _ in range(self.workers)]
+        self.pool = ThreadPoolExecutor(self.workers)
+        self.device = torch.cuda.current_device()
         self.buf = []
         for k, E in kmcs:
-            n = k.N
             # the library's pinned host arrays, filled in place (no staging copies)
             hb = k.host_buffers(1)
             hb["current_sites"][:] = 0
@@ -648,27 +659,62 @@ class HostRound:
         self.proposals = 0
         self.h2d = 0
         self.d2h = 0
+        # thread-seconds summed over the workers (they overlap in time)
         self.phase = {"host_proposals": 0.0, "propose_with_dats": 0.0, "select_accept": 0.0}
 
-    def run(self, kmc_list=None):
+    def close(self):
+        """Free the staging arrays while the workers' streams exist (a pinned array records
+        the streams it was copied on when it is freed), bind every system back to the
+        caller's stream, then end the workers' streams."""
+        import gc
+        import torch
+        self.pool.shutdown()
+        self.buf = []
+        for k, _ in self.kmcs:
+            k.release_host_buffers()
+        gc.collect()
+        torch.cuda.synchronize()
+        for k, _ in self.kmcs:
+            k._set_stream()
+        for st in self.streams:
+            st.close()
+
+    def _work(self, w):
+        import torch
+        torch.cuda.set_device(self.device)
         pc = time.perf_counter
-        for (k, E), (smc, sites, masks, diffs, prop) in zip(self.kmcs, self.buf):
-            t0 = pc()
-            pos = k.positions if isinstance(k.positions, np.ndarray) else np.asarray(k._positions_host())
-            offlattice_proposals(np.asarray(pos, dtype=np.float64).reshape(-1, 3), E, self.rng, out=prop)
-            t1 = pc()
-            k.propose_with_dats(smc, sites, prop, masks, diffs)
-            t2 = pc()
-            pid = int(self.rng.integers(0, k.N))
-            if self.rng.uniform() < np.exp(-C4_BETA * diffs[pid, 0]):
-                k.accept((pid, prop[pid].copy()))
-            t3 = pc()
-            self.phase["host_proposals"] += t1 - t0
-            self.phase["propose_with_dats"] += t2 - t1
-            self.phase["select_accept"] += t3 - t2
-            self.proposals += k.N
-            self.h2d += smc.nbytes + sites.nbytes + prop.nbytes + masks.nbytes + diffs.nbytes
-            self.d2h += diffs.nbytes + 16
+        rng = self.rngs[w]
+        ph = {key: 0.0 for key in self.phase}
+        nprop = h2d = d2h = 0
+        with torch.cuda.stream(self.streams[w].stream):
+            for j in range(w, len(self.kmcs), self.workers):
+                (k, E), (smc, sites, masks, diffs, prop) = self.kmcs[j], self.buf[j]
+                t0 = pc()
+                pos = k.positions if isinstance(k.positions, np.ndarray) else np.asarray(k._positions_host())
+                offlattice_proposals(np.asarray(pos, dtype=np.float64).reshape(-1, 3), E, rng, out=prop)
+                t1 = pc()
+                k.propose_with_dats(smc, sites, prop, masks, diffs)
+                t2 = pc()
+                pid = int(rng.integers(0, k.N))
+                if rng.uniform() < np.exp(-C4_BETA * diffs[pid, 0]):
+                    k.accept((pid, prop[pid].copy()))
+                t3 = pc()
+                ph["host_proposals"] += t1 - t0
+                ph["propose_with_dats"] += t2 - t1
+                ph["select_accept"] += t3 - t2
+                nprop += k.N
+                h2d += smc.nbytes + sites.nbytes + prop.nbytes + masks.nbytes + diffs.nbytes
+                d2h += diffs.nbytes + 16
+            self.streams[w].stream.synchronize()  # the last accept
+        return ph, nprop, h2d, d2h
+
+    def run(self):
+        for ph, nprop, h2d, d2h in self.pool.map(self._work, range(self.workers)):
+            for key in ph:
+                self.phase[key] += ph[key]
+            self.proposals += nprop
+            self.h2d += h2d
+            self.d2h += d2h
 
 
 def make_slots(reqs, kmcs, autotune=False):
@@ -850,13 +896,17 @@ def bench_config4(args, rank, world, local):
         torch.cuda.synchronize()
         e2e_dt = time.perf_counter() - t1
         nr = max(args.e2e_steps, 1)
+        hr.close()
         extras["e2e"] = {"value": (hr.proposals - p0) / e2e_dt, "unit": UNIT,
                          "h2d_bytes_per_step": int((hr.h2d - b0) / nr), "d2h_bytes_per_step": int((hr.d2h - c0) / nr),
                          "steps": args.e2e_steps,
-                         "phases_s_per_round": {k: (hr.phase[k] - ph0[k]) / nr for k in hr.phase},
+                         "round_s": e2e_dt / nr,
+                         "phases_thread_s_per_round": {k: (hr.phase[k] - ph0[k]) / nr for k in hr.phase},
+                         "workers": hr.workers,
                          "path": "KMCFMM.propose_with_dats with numpy buffers (pinned staging, H2D of every "
                                  "proposal array, D2H of the differences) + host Metropolis + KMCFMM.accept, "
-                                 "every system every round"}
+                                 "every system every round, systems taken in turn by 16 worker threads (own "
+                                 "CUDA stream and generator each)"}
     slots, tuned = make_slots(reqs, kmcs, autotune=True)
     launches = launches_per_step(slots) if not args.no_extras else None
     srv = Server(precision=prec, n_workers=args.workers)
@@ -1050,10 +1100,13 @@ def bench_config2_extra(args, rank, local):
     for prec, nsteps in (("mixed_fp64_accept", args.steps), ("fp64", max(5, args.steps // 3)),
                          ("mixed", args.steps)):
         _, k, d, _ = make_system(SIDE, rank, prec, local)
+        # launch shapes tuned on the handle (bit-identical variants), for every arm
+        d.step(1)
+        tuned = {str(key): v for key, v in k.autotune(reps=5).items() if v}
         ps, npr, _, _ = timed_loop(k, d, nsteps, 3, flush)
         out[prec] = {"value": npr / (ps.sum() * 1e-3), "ms_per_step": float(ps.mean()),
                      "p50_ms": float(np.percentile(ps, 50)), "p99_ms": float(np.percentile(ps, 99)),
-                     "steps": len(ps)}
+                     "steps": len(ps), "tuned": tuned}
         d.free()
         k.free()
     out["mixed_fp64_accept"]["vs_fp64"] = out["mixed_fp64_accept"]["value"] / out["fp64"]["value"]
@@ -1212,6 +1265,8 @@ def main_lattice48(args, world, rank, local):
     side = args.side
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     hs, kmc, drv, init_s = make_system(side, rank, args.precision, local)
+    drv.step(1)
+    kmc.autotune(reps=5)  # bit-identical launch-shape variants, the fastest kept
     if world > 1:
         dist.barrier()
     per_step, nprop, launches, clk = timed_loop(kmc, drv, args.steps, args.warmup, flush, ClockSampler(local),

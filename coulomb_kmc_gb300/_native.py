@@ -51,6 +51,17 @@ class KmcDriverParams(ctypes.Structure):
 
 KMC_DRIVE = {"lattice": 0, "offlattice": 1}
 # tuning keys (include/kmc_gb300.h)
+KMC_TUNE_P2L_GROUPS = 0
+KMC_TUNE_LR_FUSED = 1
+KMC_TUNE_LR_STAGE = 2
+KMC_TUNE_NEAR_SCALAR = 3
+KMC_TUNE_NEAR_CHUNK = 4
+KMC_TUNE_LR_NOCACHE = 5
+KMC_TUNE_P2L_FP32_FROM = 6
+KMC_TUNE_DRIVER_SERIAL = 7
+KMC_TUNE_FSELF_GENERIC = 8
+KMC_TUNE_P2L_PAIR = 9
+KMC_TUNE_P2L64 = 10
 KMC_TUNE_P2L64_CELLS = 11
 KMC_TUNE_LR_THREADS = 12
 KMC_TUNE_NEAR_SPLIT = 13

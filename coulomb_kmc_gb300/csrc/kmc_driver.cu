@@ -470,7 +470,8 @@ int prepare_branch(void *ctx, void *stream) { return enqueue_prepare((kmc_driver
 // lattice), while beside the double-FP32 accept they hide (0.38 -> 0.31 ms).
 bool pipelined(const kmc_driver *d)
 {
-    return kmc_int_tuning(d->sys, KMC_TUNE_DRIVER_SERIAL) != 1 && kmc_int_accept_df32(d->sys);
+    const int t = kmc_int_tuning(d->sys, KMC_TUNE_DRIVER_SERIAL);
+    return t == 2 || (t == 0 && kmc_int_accept_df32(d->sys));
 }
 
 // before a replay or capture of a pipelined step: it expects prepared proposals

@@ -252,6 +252,13 @@ class KMCFMM:
             out[key] = h[:n * shape[1]].numpy().reshape(shape)
         return out
 
+    def release_host_buffers(self):
+        """Drop the pinned staging arrays (those host_buffers returns) and their device
+        twins; the next host-path call allocates them again.  A caller that ran the host
+        path on CUDA streams it is about to destroy calls this first: a pinned array
+        records, when freed, the streams its copies ran on."""
+        self._staging = {}
+
     def propose_with_dats(self, site_max_counts, current_sites, prop_positions, prop_masks, prop_energy_diffs,
                           diff=True, prop_charges=None, sync=True):
         """Energy differences of masked proposals written into prop_energy_diffs (kmc_fmm.py:665-762).

@@ -243,7 +243,8 @@ int kmc_inject(kmc_system *s, int64_t n, const double *positions, const double *
 #define KMC_TUNE_NEAR_CHUNK 4  /* mixed near field: neighbours staged per chunk, 0 128, 1 256 */
 #define KMC_TUNE_LR_NOCACHE 5  /* mixed pbc lattice term: 0 h = A b kept per charge between moves, 1 recomputed each propose */
 #define KMC_TUNE_P2L_FP32_FROM 6 /* double-FP32 accept: orders l >= k in FP32 (0: k = 6; k >= l: none) */
-#define KMC_TUNE_DRIVER_SERIAL 7 /* device driver: 0 next step's set-up beside the accept, 1 plain order */
+#define KMC_TUNE_DRIVER_SERIAL 7 /* device driver: 0 next step's set-up beside a double-FP32 accept, plain order
+                                    beside an FP64 one; 1 plain order; 2 set-up beside every accept */
 #define KMC_TUNE_FSELF_GENERIC 8 /* mixed pbc lattice self term: 0 unrolled L = 12 cubic evaluator, 1 interpreter */
 #define KMC_TUNE_P2L_PAIR 9 /* double-FP32 accept at L = 12, orders from 6 in FP32: 0 column-pair kernel, 1 per-column kernel */
 #define KMC_TUNE_P2L64 10 /* FP64 accept at L = 8, 12, 16: 0 column-pair kernel, 1 per-column kernel */
