@@ -392,9 +392,11 @@ def bench_precision_split(args):
             k.initialise()
             init_s = time.perf_counter() - t0
             d = KMCDriver(k, "lattice", BETA, seed=99, lattice_side=side, lattice_sites=hs.site_of)
+            d.step(1)
+            tuned = {str(key): v for key, v in k.autotune(reps=3).items() if v}  # bit-identical shapes, per arm
             ps, npr, _, _ = timed_loop(k, d, args.steps, args.warmup, flush)
             res[prec] = {"value": npr / (ps.sum() * 1e-3), "ms_per_step": float(ps.mean()), "init_s": init_s,
-                         "p99_ms": float(np.percentile(ps, 99))}
+                         "p99_ms": float(np.percentile(ps, 99)), "tuned": tuned}
             d.free()
             k.free()
         err = error_stats(side, r6, Lx, seed=2, nsteps=args.error_steps, precision=args.precision)
@@ -872,6 +874,17 @@ def offlattice_flop_model(kmc, L_):
     return 2 * pair + 2 * len(cells) * far, float(np.mean(nb[cells]))
 
 
+def offlattice_flops_executed(kmc, L_):
+    """The part of offlattice_flop_model the kernel executes with the moving charges'
+    near-field potentials kept between moves: the new side's pair terms, both sides'
+    cell-expansion evaluations."""
+    total, mnb = offlattice_flop_model(kmc, L_)
+    nh = L_ * (L_ + 1) // 2
+    far = 12 * nh + 6 * L_
+    n = kmc.N
+    return 0.5 * (total - 2 * n * far) + 2 * n * far
+
+
 def bench_config4(args, rank, world, local):
     """The headline: batched replicas of the metric's configuration (see config4_requests)."""
     import torch
@@ -915,13 +928,18 @@ def bench_config4(args, rank, world, local):
     # blocks per cell of the near field repeat each cell's set-up per block: tuned on whole
     # rounds (bit-identical candidates; the rounds are untimed warm-up rounds)
     split, split_ms = srv.autotune_key(slots, _native.KMC_TUNE_NEAR_SPLIT, (1, 2), rounds=2)
-    # so is the residency of the FP64 accept kernel (blocks per SM, 0 = no limit), which
-    # decides how much of each SM the other systems' near-field kernels find free
-    per_sm, per_sm_ms = srv.autotune_key(slots, _native.KMC_TUNE_P2L64_PER_SM, (0, 1, 2), rounds=2)
+    # so are the FP64 accept kernel's cells per block and residency (blocks per SM), which
+    # decide how much of each SM the other systems' near-field kernels find free ({}: each
+    # size bucket's own kmc_autotune choice, no residency limit)
+    k_c, k_s = _native.KMC_TUNE_P2L64_CELLS, _native.KMC_TUNE_P2L64_PER_SM
+    combos = [{}, {k_s: 1}, {k_c: 2, k_s: 2}, {k_c: 2, k_s: 3}]
+    best, combo_ms = srv.autotune_keys(slots, combos, rounds=2)
+    per_sm = {str(k): v for k, v in combos[best].items()}
+    per_sm_ms = {json.dumps({str(k): v for k, v in c.items()}): t for c, t in zip(combos, combo_ms)}
     mode, mode_ms = srv.autotune_launch(slots, rounds=3)
     extras["autotune"] = {"kernel_launch_shapes": tuned, "near_blocks_per_cell": split,
                           "round_ms_by_near_blocks_per_cell": split_ms,
-                          "fp64_accept_blocks_per_sm": per_sm, "round_ms_by_fp64_accept_blocks_per_sm": per_sm_ms,
+                          "fp64_accept_shape": per_sm, "round_ms_by_fp64_accept_shape": per_sm_ms,
                           "round_launch": mode, "round_ms_by_launch": mode_ms}
     if world > 1:
         import torch.distributed as dist
@@ -955,7 +973,8 @@ def bench_config4(args, rank, world, local):
             per_launch = {k: v[0] / max(v[1], 1) for k, v in kt.items() if v[1] > 0}
             fl, mnb = offlattice_flop_model(sl.kmc, 12)
             big[bc] = {"n": reqs[i].n, "per_kernel_ms": {k: round(v, 5) for k, v in per_launch.items()},
-                       "near_flops": fl, "mean_neighbours": mnb}
+                       "near_flops": fl, "near_flops_executed": offlattice_flops_executed(sl.kmc, 12),
+                       "mean_neighbours": mnb}
         srv.free_buckets()
         free_slots(slots)
         peak64, peak32 = fma_peak(True), fma_peak(False)
@@ -972,6 +991,11 @@ def bench_config4(args, rank, world, local):
             "flops_convention": "algorithmic flops of the FP64 algorithm (add/mul 1, FMA 2, rsqrt 1); the mixed "
                                 "kernel spends several FP32 instructions per algorithmic flop",
             "flops_per_launch": b["near_flops"], "mean_neighbours_per_proposal": b["mean_neighbours"],
+            "flops_executed_per_launch": b["near_flops_executed"],
+            "frac_executed": (b["near_flops_executed"] / (nf_ms * 1e-3) / 1e12 / peak32) if nf_ms else None,
+            "executed_note": "the survey's algorithmic count takes every moving charge's old-side pair terms; "
+                             "with the near-field potentials kept between moves the kernel executes the new "
+                             "side's pair terms and both sides' cell-expansion evaluations only",
             "per_kernel_ms_largest": {k: v["per_kernel_ms"] for k, v in big.items()},
             "traffic_note": "not captured in this run; the ncu captures summarised with the profiles give the "
                             "DRAM bytes per launch"}

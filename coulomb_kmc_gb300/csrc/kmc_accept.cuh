@@ -150,8 +150,9 @@ constexpr int kMgBlocks = 8, kMgThreads = 128;
 
 // DF (the mixed paths): the increments of M and the rows of g in double-FP32 on the
 // FP32 pipe (FP64 dependency chains are slow on GB300; ~48-bit significands keep g and
-// M within ~1e-14 of the FP64 forms), with the operator's FP64 entries split into
-// FP32 pairs at set-up (a2_val, ai2_val).
+// M within ~1e-14 of the FP64 forms), in box units (coordinates x / E, the operator
+// A E^(l + l' + 1) split into FP32 pairs at set-up: a2_val, ai2_val), which keeps every
+// value in the FP32 range for any box up to l = 20.
 template <bool DF>
 __global__ void __launch_bounds__(kMgThreads) k_accept_mpole_g(Sys S, Props P, const AcceptRec *rec,
                                                               unsigned *ticket)
@@ -183,7 +184,10 @@ __global__ void __launch_bounds__(kMgThreads) k_accept_mpole_g(Sys S, Props P, c
         for (int pass = 0; pass < 2; ++pass) {
             const double x = pass == 0 ? r.xo : r.xn, y = pass == 0 ? r.yo : r.yn, z = pass == 0 ? r.zo : r.zn;
             if (DF) {
-                const df32 xd = df_from_double(x), yd = df_from_double(y), zd = df_from_double(z);
+                // at x / E (box units: the harmonics of position-unit coordinates leave the
+                // FP32 range for large boxes at high orders), scaled back by E^l in FP64
+                const df32 xd = df_from_double(x * S.inv_E), yd = df_from_double(y * S.inv_E),
+                           zd = df_from_double(z * S.inv_E);
                 const df32 r2 = df_add(df_add(df_mul(xd, xd), df_mul(yd, yd)), df_mul(zd, zd));
                 df32 dre = df_make(1.0f, 0.0f), dim = df_make(0.0f, 0.0f);
                 for (int k = 1; k <= m; ++k) {
@@ -204,8 +208,9 @@ __global__ void __launch_bounds__(kMgThreads) k_accept_mpole_g(Sys S, Props P, c
                     cre = nre;
                     cim = nim;
                 }
-                dv[pass][0] = df_to_double(cre);
-                dv[pass][1] = df_to_double(cim);
+                const double sc = S.escale[h] * S.inv_E;
+                dv[pass][0] = df_to_double(cre) * sc;
+                dv[pass][1] = df_to_double(cim) * sc;
             } else {
                 const double r2 = x * x + y * y + z * z;
                 double dre = 1.0, dim = 0.0;
@@ -239,7 +244,9 @@ __global__ void __launch_bounds__(kMgThreads) k_accept_mpole_g(Sys S, Props P, c
         v.y += -r.q * dv[1][1];
         mgs[h] = v;
         if (DF) {
-            const df32 vr = df_from_double(v.x), vi = df_from_double(v.y);
+            // in box units, M E^-(l + 1), against the box-unit operator pairs
+            const double ie = 1.0 / S.escale[h];
+            const df32 vr = df_from_double(v.x * ie), vi = df_from_double(v.y * ie);
             m2[h] = make_float4(vr.hi, vi.hi, vr.lo, vi.lo);
         }
     }
@@ -262,7 +269,11 @@ __global__ void __launch_bounds__(kMgThreads) k_accept_mpole_g(Sys S, Props P, c
                 t = df_add(t, df_make(__shfl_xor_sync(0xffffffffu, t.hi, off), __shfl_xor_sync(0xffffffffu, t.lo, off)));
                 u = df_add(u, df_make(__shfl_xor_sync(0xffffffffu, u.hi, off), __shfl_xor_sync(0xffffffffu, u.lo, off)));
             }
-            if (lane == 0) P.g[row] = make_double2(df_to_double(t), df_to_double(u));
+            // box units: sum A E^(l + l' + 1) M E^-(l' + 1) = E^l (A M)_row
+            if (lane == 0) {
+                const double sc = S.E / S.escale[row];
+                P.g[row] = make_double2(df_to_double(t) * sc, df_to_double(u) * sc);
+            }
         } else {
             double t = 0.0, u = 0.0;
             for (int k = S.ar_ptr[row] + lane; k < S.ar_ptr[row + 1]; k += 32) t += S.ar_val[k] * mgs[S.ar_col[k]].x;

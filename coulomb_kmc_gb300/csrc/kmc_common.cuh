@@ -66,7 +66,7 @@ struct Sys {
     float4 *st_hi, *st_lo;       // [ncell][cap] near-field copy: position relative to the slot's cell
                                  // centre in cell widths (grid_split), charge as df32
     float4 *lexp32;              // [ncell][NH] (re_hi, im_hi, re_lo, im_lo)
-    const float2 *a2_val;        // the folded form's FP64 entries as FP32 pairs (pattern of ar / ai)
+    const float2 *a2_val;        // the folded form in box units, A E^(l + l' + 1), as FP32 pairs (pattern of ar / ai)
     const float2 *ai2_val;
     const float *ar32_val;       // full folded lattice form in FP32 (pattern of ar / ai)
     const float *ai32_val;

@@ -374,6 +374,12 @@ class KMCFMM:
         """Set one launch-shape tuning key (kmc_set_tuning)."""
         _native.check(_native.lib().kmc_set_tuning(self._handle, int(key), int(value)), "kmc_set_tuning")
 
+    def get_tuning(self, key):
+        """The value of one launch-shape tuning key (kmc_get_tuning; 0: the built-in choice)."""
+        v = ctypes.c_int32()
+        _native.check(_native.lib().kmc_get_tuning(self._handle, int(key), ctypes.byref(v)), "kmc_get_tuning")
+        return int(v.value)
+
     def reserve_store(self, capacity):
         """Set the cell store's capacity (slots per cell) to at least ``capacity`` and the
         largest occupancy (kmc_store_reserve); returns the new capacity.  Synchronises; a

@@ -229,6 +229,29 @@ class Server:
             s.done += 1
         return e0.elapsed_time(e1)
 
+    def autotune_keys(self, slots, candidates, rounds=2):
+        """autotune_key for combinations: each candidate maps keys to values, a key it
+        leaves out keeps every system's own value (an empty candidate: the systems as
+        they are).  Returns (the best candidate's index, [median round ms per candidate])."""
+        keys = sorted({k for c in candidates for k in c})
+        base = [{k: sl.kmc.get_tuning(k) for k in keys} for sl in slots]
+
+        def apply(c):
+            for sl, b in zip(slots, base):
+                for k in keys:
+                    sl.kmc.set_tuning(k, c.get(k, b[k]))
+                sl.drv.capture()
+            self.free_buckets()
+
+        timing = []
+        for c in candidates:
+            apply(c)
+            self.round(slots)
+            timing.append(float(np.median([self.round(slots) for _ in range(rounds)])))
+        best = int(np.argmin(timing))
+        apply(candidates[best])
+        return best, timing
+
     def autotune_key(self, slots, key, candidates, rounds=2):
         """Tune one launch-shape key whose variants give bit-identical results on whole
         rounds of `slots` (the device full, as in service): each candidate is set on

@@ -127,3 +127,41 @@ def test_bucket_rounds_equal_stream_rounds():
     for a, b in zip(res["streams"], res["buckets"]):
         assert a[0] == b[0] and a[1] == b[1]
         assert np.array_equal(a[2], b[2])
+
+
+def test_round_tuner_keeps_results_and_each_systems_own_values():
+    """Server.autotune_keys over combinations of the FP64 accept's cells per block and
+    residency: the rounds it times are real rounds, the systems end as untuned ones
+    do after the same number of rounds, and a candidate that leaves a key out keeps
+    every system's own value."""
+    reqs = [Request(rid=i, kind="offlattice", bc="pbc" if i % 2 else "free_space", n=1500 + 400 * i, rounds=8,
+                    seed=60 + i) for i in range(4)]
+    kc, ks = _native.KMC_TUNE_P2L64_CELLS, _native.KMC_TUNE_P2L64_PER_SM
+    res = {}
+    for tuned in (False, True):
+        srv = Server(precision="mixed_fp64_accept", n_workers=4)
+        slots = []
+        for r in reqs:
+            k, d = build_system(r, "mixed_fp64_accept")
+            k.set_tuning(kc, 4)  # each system's own value, kept by the empty candidate
+            slots.append(Slot(req=r, kmc=k, drv=d, nbytes=0, admitted=0.0))
+        n_rounds = 0
+        if tuned:
+            combos = [{}, {ks: 1}, {kc: 2, ks: 3}]
+            best, ms = srv.autotune_keys(slots, combos, rounds=1)
+            assert len(ms) == 3 and 0 <= best < 3
+            n_rounds = 3 * 2
+            want = {kc: 4, ks: 0}
+            want.update(combos[best])
+            for sl in slots:
+                assert sl.kmc.get_tuning(kc) == want[kc] and sl.kmc.get_tuning(ks) == want[ks]
+        for _ in range(8 - n_rounds):
+            srv.round(slots)
+        res[tuned] = [(sl.kmc.energy, sl.drv.stats(), sl.kmc.state()["positions"]) for sl in slots]
+        srv.free_buckets()
+        for sl in slots:
+            sl.drv.free()
+            sl.kmc.free()
+    for a, b in zip(res[False], res[True]):
+        assert a[0] == b[0] and a[1] == b[1]
+        assert np.array_equal(a[2], b[2])
