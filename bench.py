@@ -616,6 +616,14 @@ def build_kmcs(reqs, precision, threads=4):
     return out
 
 
+def apply_tune(k, args):
+    """Launch-shape keys given on the command line (--tune KEY=VALUE ...), set on a system
+    before its steps are captured."""
+    for kv in args.tune:
+        key, val = kv.split("=")
+        k.set_tuning(int(key), int(val))
+
+
 def offlattice_proposals(pos, E, rng, out=None):
     """One displacement per charge, uniform in [-step, step]^3, re-drawn (the same draws
     in the same order) for the rows that left the box; only those rows are re-checked.
@@ -894,6 +902,8 @@ def bench_config4(args, rank, world, local):
     prec = args.precision
     t0 = time.perf_counter()
     kmcs = build_kmcs(reqs, prec, threads=args.build_threads)
+    for k, _ in kmcs:
+        apply_tune(k, args)
     build_s = time.perf_counter() - t0
     extras = {}
     # e2e: the reference-facing API with host buffers (before the device drivers exist)
@@ -1153,10 +1163,12 @@ def bench_single(args):
         bc = "pbc" if args.case == "c4pbc" else "free_space"
         big = max((r for r in reqs if r.bc == bc), key=lambda r: r.n)
         (k, E), = build_kmcs([big], args.precision, threads=1)
+        apply_tune(k, args)
         d = KMCDriver(k, "offlattice", C4_BETA, seed=big.seed, step=C4_STEP)
         what = f"{bc} off-lattice N={big.n}"
     else:
         _, k, d, _ = make_system(SIDE, 0, args.precision, 0)
+        apply_tune(k, args)
         what = f"pbc lattice-hop {SIDE}^3"
     d.step(2)
     torch.cuda.synchronize()
@@ -1214,6 +1226,8 @@ def main():
     ap.add_argument("--build-threads", type=int, default=4)
     ap.add_argument("--ref-steps", type=int, default=10)
     ap.add_argument("--no-extras", action="store_true", help="timed loop only (for profiler runs)")
+    ap.add_argument("--tune", nargs="*", default=[], metavar="KEY=VALUE",
+                    help="launch-shape tuning keys (include/kmc_gb300.h KMC_TUNE_*) set on every system")
     ap.add_argument("--no-graph", action="store_true", help="launch the step eagerly instead of a CUDA graph")
     ap.add_argument("--workload", default="batched",
                     choices=["batched", "lattice48", "precision_split", "batched_streams", "serving", "drift",

@@ -1065,7 +1065,7 @@ int propose_evaluate(kmc_system *s, int64_t n_old_grid, int64_t n_new_grid, doub
     if (S.mixed) {
         // 128 staged neighbours per chunk keep a one-warp block near 7 KB of shared
         // memory, so about 28 blocks fit an SM and a 4,096-cell grid runs in one wave
-        const int chunk = s->tune[KMC_TUNE_NEAR_CHUNK] == 1 ? 256 : 128;
+        const int chunk = s->tune[KMC_TUNE_NEAR_CHUNK] == 1 ? 256 : (s->tune[KMC_TUNE_NEAR_CHUNK] == 2 ? 64 : 128);
         const size_t smem =
             chunk * (2 * sizeof(float4) + 2 * sizeof(int) + sizeof(unsigned long long)) + (size_t)S.NH * sizeof(float4);
         LaunchScope ls(s, K_NEAR_CELL);
@@ -1080,6 +1080,10 @@ int propose_evaluate(kmc_system *s, int64_t n_old_grid, int64_t n_new_grid, doub
             k_near_cell_mixed<false, 128><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split, kept);
         else if (chunk == 256)
             k_near_cell_mixed<true, 256><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split, kept);
+        else if (chunk == 64 && S.L == 12)
+            k_near_cell_mixed<true, 64, 12><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split, kept);
+        else if (chunk == 64)
+            k_near_cell_mixed<true, 64><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split, kept);
         else
             if (S.L == 12)
                 k_near_cell_mixed<true, 128, 12><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split, kept);

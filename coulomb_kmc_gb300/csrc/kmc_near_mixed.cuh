@@ -261,7 +261,9 @@ constexpr int kNearMixedThreads = 32;
 // accept), so they only evaluate the cell expansion; otherwise they are items of the
 // pair loop like the proposals
 template <bool PACKED, int CHUNK, int LT = 0>
-__global__ void __launch_bounds__(kNearMixedThreads) k_near_cell_mixed(const Sys S, Props P, const bool self_in_lr,
+// Registers held to what the residency allows: CHUNK 64 (~4.3 KB of shared memory) at most
+// 64 a thread, so 32 blocks (the SM's limit) fit an SM; 27 blocks otherwise (~7.4 KB)
+__global__ void __launch_bounds__(kNearMixedThreads, CHUNK <= 64 ? 32 : 27) k_near_cell_mixed(const Sys S, Props P, const bool self_in_lr,
                                                                         const int split, const bool kept)
 {
     extern __shared__ float4 msm[];

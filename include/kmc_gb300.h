@@ -138,8 +138,8 @@ int kmc_accept_device(kmc_system *s, const int64_t *d_pid, const double *d_new_p
  * 4096 moving charges and 16384 proposals per call (larger calls return
  * KMC_EINVAL with a message).  Set-up: the first call on a device (and the
  * first after that device's context was replaced) looks up the array's device
- * address (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture.  Every call on a device shares the array and it
+ * address (cudaGetSymbolAddress) with that device current.  Every call on a
+ * device shares the array and it
  * keeps the last call's contents, so calls that overlap on the GPU (different
  * streams or handles) race; serialise them.  Each call writes every element of
  * it that the call reads.  Inputs are checked on the device before use: ids
@@ -240,7 +240,7 @@ int kmc_inject(kmc_system *s, int64_t n, const double *positions, const double *
 #define KMC_TUNE_LR_FUSED 1   /* mixed pbc lattice term: 0 per-charge and per-proposal kernels, 1 one fused kernel */
 #define KMC_TUNE_LR_STAGE 2   /* fused lattice kernel: 0 folded form in shared memory (when it fits), 1 read-only cache */
 #define KMC_TUNE_NEAR_SCALAR 3 /* mixed near field: 0 two neighbours per packed FP32 instruction, 1 one at a time */
-#define KMC_TUNE_NEAR_CHUNK 4  /* mixed near field: neighbours staged per chunk, 0 128, 1 256 */
+#define KMC_TUNE_NEAR_CHUNK 4  /* mixed near field: neighbours staged per chunk, 0 128, 1 256, 2 64 */
 #define KMC_TUNE_LR_NOCACHE 5  /* mixed pbc lattice term: 0 h = A b kept per charge between moves, 1 recomputed each propose */
 #define KMC_TUNE_P2L_FP32_FROM 6 /* double-FP32 accept: orders l >= k in FP32 (0: k = 6; k >= l: none) */
 #define KMC_TUNE_DRIVER_SERIAL 7 /* device driver: 0 next step's set-up beside a double-FP32 accept, plain order
