@@ -114,7 +114,7 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 def flop_model(kmc, host_sys, lr_nnz_folded):
     """Algorithmic FP64 flops per launch of the step's kernels (add/mul = 1,
-    FMA = 2, rsqrt = 1; the counting convention of the survey), from this step's
+    FMA = 2, rsqrt = 1), from this step's
     proposals and cell occupancy."""
     st = kmc.state()
     n = 2 ** (R - 1)
@@ -852,7 +852,7 @@ def launches_per_step(slots):
 def offlattice_flop_model(kmc, L_):
     """Algorithmic flops of one launch of the mixed near-field kernel (near_far_cell) on an
     off-lattice system: every charge's proposal (new side) and old position (old side)
-    against its 27 neighbour cells, plus the cell-expansion evaluation (survey counting
+    against its 27 neighbour cells, plus the cell-expansion evaluation (counting
     convention: add/mul 1, FMA 2, rsqrt 1)."""
     st = kmc.state()
     n = round(len(st["occupancy"]) ** (1 / 3))
@@ -1003,7 +1003,7 @@ def bench_config4(args, rank, world, local):
             "flops_per_launch": b["near_flops"], "mean_neighbours_per_proposal": b["mean_neighbours"],
             "flops_executed_per_launch": b["near_flops_executed"],
             "frac_executed": (b["near_flops_executed"] / (nf_ms * 1e-3) / 1e12 / peak32) if nf_ms else None,
-            "executed_note": "the survey's algorithmic count takes every moving charge's old-side pair terms; "
+            "executed_note": "the algorithmic count takes every moving charge's old-side pair terms; "
                              "with the near-field potentials kept between moves the kernel executes the new "
                              "side's pair terms and both sides' cell-expansion evaluations only",
             "per_kernel_ms_largest": {k: v["per_kernel_ms"] for k, v in big.items()},
