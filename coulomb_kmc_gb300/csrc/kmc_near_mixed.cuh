@@ -42,12 +42,10 @@ __global__ void k_refresh_lexp32(const Sys S)
 // with compensated accumulation; self term: moved pair in df32, images in FP32.
 // Results are written as FP64 (hi + lo).
 // ---------------------------------------------------------------------------
-// LT > 0: the order is the compile-time LT (loops unrolled, table offsets constant).
-// Not inlined: the near kernel calls it for the moving charges and for the proposals,
-// and one copy of the unrolled body keeps the kernel's instruction footprint down
+// LT > 0: the order is the compile-time LT (loops unrolled, table offsets constant)
 template <int LT = 0>
-__device__ __noinline__ df32 far_eval_mixed(const float4 *Lc, const int Lr, const df32 x, const df32 y,
-                                            const df32 z)
+__device__ __forceinline__ df32 far_eval_mixed(const float4 *Lc, const int Lr, const df32 x, const df32 y,
+                                               const df32 z)
 {
     const int L = LT > 0 ? LT : Lr;
     // FP32 part, l >= 3
