@@ -627,10 +627,16 @@ def apply_tune(k, args):
 def offlattice_proposals(pos, E, rng, out=None):
     """One displacement per charge, uniform in [-step, step]^3, re-drawn (the same draws
     in the same order) for the rows that left the box; only those rows are re-checked.
-    `out`: an (N, 3) array to write into."""
+    `out`: an (N, 3) array to write into.  The draws are formed in place (the values
+    rng.uniform(-step, step) gives: -step + 2 step u), with no temporary arrays."""
     h = 0.5 * E
-    prop = np.add(pos, rng.uniform(-C4_STEP, C4_STEP, size=pos.shape), out=out)
-    bad = np.flatnonzero(np.any(np.abs(prop) > h, axis=1))
+    prop = out if out is not None else np.empty_like(pos)
+    rng.random(out=prop)
+    prop *= 2 * C4_STEP
+    prop -= C4_STEP
+    prop += pos
+    flat = prop.reshape(-1)
+    bad = np.unique(np.flatnonzero((flat > h) | (flat < -h)) // 3)
     while bad.size:
         prop[bad] = pos[bad] + rng.uniform(-C4_STEP, C4_STEP, size=(bad.size, 3))
         bad = bad[np.any(np.abs(prop[bad]) > h, axis=1)]
