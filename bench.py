@@ -616,6 +616,20 @@ def build_kmcs(reqs, precision, threads=4):
     return out
 
 
+def combine_ranks(t_ms, nprop, device):
+    """Across the replicas (one per rank, no exchange in the timed work): the slowest
+    rank's timed milliseconds and the proposals of all ranks, so that the whole-job value
+    is all proposals over the slowest rank's time."""
+    import torch
+    import torch.distributed as dist
+    tot = torch.tensor([t_ms, float(nprop)], dtype=torch.float64, device=device)
+    tmax = tot[0:1].clone()
+    nsum = tot[1:2].clone()
+    dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+    dist.all_reduce(nsum, op=dist.ReduceOp.SUM)
+    return float(tmax[0]), float(nsum[0])
+
+
 def apply_tune(k, args):
     """Launch-shape keys given on the command line (--tune KEY=VALUE ...), set on a system
     before its steps are captured."""
@@ -967,12 +981,7 @@ def bench_config4(args, rank, world, local):
                       "round_ms_p99": float(np.percentile(ms, 99)), "build_s": build_s,
                       "e2e": extras.get("e2e", {}).get("value")}), file=sys.stderr, flush=True)
     if world > 1:
-        import torch.distributed as dist
-        tot = torch.tensor([t_ms, float(nprop)], dtype=torch.float64, device="cuda")
-        tmax = tot[0:1].clone()
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        dist.all_reduce(tot[1:2], op=dist.ReduceOp.SUM)
-        t_ms, nprop = float(tmax[0]), float(tot[1])
+        t_ms, nprop = combine_ranks(t_ms, nprop, "cuda")
         value = nprop / (t_ms * 1e-3)
     if not args.no_extras:
         # per-kernel times of the largest system of each boundary condition (separate pass)
@@ -1318,13 +1327,9 @@ def main_lattice48(args, world, rank, local):
     if world > 1:
         dist.barrier()
     t_ms = float(per_step.sum())
-    tot = torch.tensor([t_ms, float(nprop)], dtype=torch.float64, device="cuda")
+    nprop_all = float(nprop)
     if world > 1:
-        tmax = tot[0:1].clone()
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        dist.all_reduce(tot[1:2], op=dist.ReduceOp.SUM)
-        tot[0] = tmax[0]
-    t_ms, nprop_all = float(tot[0]), float(tot[1])
+        t_ms, nprop_all = combine_ranks(t_ms, nprop, "cuda")
     value = nprop_all / (t_ms * 1e-3)
 
     extras = {}
