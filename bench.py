@@ -641,16 +641,10 @@ def apply_tune(k, args):
 def offlattice_proposals(pos, E, rng, out=None):
     """One displacement per charge, uniform in [-step, step]^3, re-drawn (the same draws
     in the same order) for the rows that left the box; only those rows are re-checked.
-    `out`: an (N, 3) array to write into.  The draws are formed in place (the values
-    rng.uniform(-step, step) gives: -step + 2 step u), with no temporary arrays."""
+    `out`: an (N, 3) array to write into."""
     h = 0.5 * E
-    prop = out if out is not None else np.empty_like(pos)
-    rng.random(out=prop)
-    prop *= 2 * C4_STEP
-    prop -= C4_STEP
-    prop += pos
-    flat = prop.reshape(-1)
-    bad = np.unique(np.flatnonzero((flat > h) | (flat < -h)) // 3)
+    prop = np.add(pos, rng.uniform(-C4_STEP, C4_STEP, size=pos.shape), out=out)
+    bad = np.flatnonzero(np.any(np.abs(prop) > h, axis=1))
     while bad.size:
         prop[bad] = pos[bad] + rng.uniform(-C4_STEP, C4_STEP, size=(bad.size, 3))
         bad = bad[np.any(np.abs(prop[bad]) > h, axis=1)]
@@ -958,6 +952,8 @@ def bench_config4(args, rank, world, local):
     # blocks per cell of the near field repeat each cell's set-up per block: tuned on whole
     # rounds (bit-identical candidates; the rounds are untimed warm-up rounds)
     split, split_ms = srv.autotune_key(slots, _native.KMC_TUNE_NEAR_SPLIT, (1, 2), rounds=2)
+    # the near field's scheduling priority (default, or the device's highest)
+    prio, prio_ms = srv.autotune_key(slots, _native.KMC_TUNE_NEAR_PRIORITY, (0, 1), rounds=2)
     # so are the FP64 accept kernel's cells per block and residency (blocks per SM), which
     # decide how much of each SM the other systems' near-field kernels find free ({}: each
     # size bucket's own kmc_autotune choice, no residency limit)
@@ -969,6 +965,7 @@ def bench_config4(args, rank, world, local):
     mode, mode_ms = srv.autotune_launch(slots, rounds=3)
     extras["autotune"] = {"kernel_launch_shapes": tuned, "near_blocks_per_cell": split,
                           "round_ms_by_near_blocks_per_cell": split_ms,
+                          "near_priority": prio, "round_ms_by_near_priority": prio_ms,
                           "fp64_accept_shape": per_sm, "round_ms_by_fp64_accept_shape": per_sm_ms,
                           "round_launch": mode, "round_ms_by_launch": mode_ms}
     if world > 1:

@@ -67,6 +67,7 @@ KMC_TUNE_LR_THREADS = 12
 KMC_TUNE_NEAR_SPLIT = 13
 KMC_TUNE_NEAR_OLD = 14
 KMC_TUNE_P2L64_PER_SM = 15
+KMC_TUNE_NEAR_PRIORITY = 16
 
 
 def _nvcc():
@@ -191,7 +192,7 @@ class DedicatedStream:
 
 
 NKERNELS = 19
-NTUNE = 16
+NTUNE = 17
 
 
 def check(rc, what):

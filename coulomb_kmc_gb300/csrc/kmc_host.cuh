@@ -8,6 +8,7 @@ struct kmc_system {
     kmc_params prm{};
     int tune[KMC_NTUNE] = {};
     int smem_sm = 0;  // shared memory per SM of the device (bytes)
+    int prio_hi = 0;  // the device's highest stream / launch priority (numerically least)
     cudaStream_t stream = nullptr;
     // side stream of the accept: the move's energy and the multipole / lattice vector
     // updates run there beside the particle-to-local kernel (fork / join events)
@@ -1074,21 +1075,34 @@ int propose_evaluate(kmc_system *s, int64_t n_old_grid, int64_t n_new_grid, doub
         // results unchanged
         const int split = s->tune[KMC_TUNE_NEAR_SPLIT] > 0 ? s->tune[KMC_TUNE_NEAR_SPLIT] : 1;
         const bool sil = lattice_takes_self(s);
+        // the mixed near field at the device's highest scheduling priority (tuning): when
+        // many systems' kernels wait for SM resources, its blocks go first and the FP64
+        // accept kernels of other systems fill what is left; results unchanged
+        const int prio = s->tune[KMC_TUNE_NEAR_PRIORITY] == 1 ? s->prio_hi : 0;
+        void (*kern)(const Sys, Props, const bool, const int, const bool);
         if (scalar && chunk == 256)
-            k_near_cell_mixed<false, 256><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split, kept);
+            kern = k_near_cell_mixed<false, 256>;
         else if (scalar)
-            k_near_cell_mixed<false, 128><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split, kept);
+            kern = k_near_cell_mixed<false, 128>;
         else if (chunk == 256)
-            k_near_cell_mixed<true, 256><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split, kept);
-        else if (chunk == 64 && S.L == 12)
-            k_near_cell_mixed<true, 64, 12><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split, kept);
+            kern = k_near_cell_mixed<true, 256>;
         else if (chunk == 64)
-            k_near_cell_mixed<true, 64><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split, kept);
+            kern = S.L == 12 ? k_near_cell_mixed<true, 64, 12> : k_near_cell_mixed<true, 64>;
         else
-            if (S.L == 12)
-                k_near_cell_mixed<true, 128, 12><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split, kept);
-            else
-                k_near_cell_mixed<true, 128><<<S.ncell * split, kNearMixedThreads, smem, s->stream>>>(S, s->P, sil, split, kept);
+            kern = S.L == 12 ? k_near_cell_mixed<true, 128, 12> : k_near_cell_mixed<true, 128>;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)(S.ncell * split));
+        cfg.blockDim = dim3(kNearMixedThreads);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = s->stream;
+        cudaLaunchAttribute attr[1];
+        if (prio != 0) {
+            attr[0].id = cudaLaunchAttributePriority;
+            attr[0].val.priority = prio;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+        }
+        KMC_CUDA(cudaLaunchKernelEx(&cfg, kern, S, s->P, sil, split, kept));
     } else {
         const size_t smem = kNearChunk * (sizeof(double4_32a) + sizeof(int)) + (size_t)S.NH * sizeof(double2);
         LaunchScope ls(s, K_NEAR_CELL);

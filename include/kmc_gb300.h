@@ -255,7 +255,9 @@ int kmc_inject(kmc_system *s, int64_t n, const double *positions, const double *
                                 accept updates the charges around the moved one), 1 summed afresh on every propose */
 #define KMC_TUNE_P2L64_PER_SM 15 /* FP64 column-pair accept: at most 1..4 blocks resident per SM (0: no limit), the rest of
                                     each SM left to other kernels; results unchanged */
-#define KMC_NTUNE 16
+#define KMC_TUNE_NEAR_PRIORITY 16 /* mixed near field: 0 default scheduling priority, 1 the device's highest (blocks
+                                    dispatched before other kernels' waiting blocks); results unchanged */
+#define KMC_NTUNE 17
 int kmc_set_tuning(kmc_system *s, int32_t key, int32_t value);
 int kmc_get_tuning(kmc_system *s, int32_t key, int32_t *value_out);
 /* Autotuner (no reference counterpart; the reference's OpenMP loops and block-256

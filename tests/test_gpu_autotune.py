@@ -89,6 +89,8 @@ def test_every_tuning_candidate_is_bit_identical():
     for val in (1, 2):
         got, _ = _run({_native.KMC_TUNE_P2L64_PER_SM: val})
         _same(ref, got)
+    got, _ = _run({_native.KMC_TUNE_NEAR_PRIORITY: 1})
+    _same(ref, got)
 
 
 def test_fp64_accept_shapes_bit_identical_in_free_space():
