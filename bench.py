@@ -683,6 +683,7 @@ class HostRound:
         self.proposals = 0
         self.h2d = 0
         self.d2h = 0
+        self.round_no = 0
         # thread-seconds summed over the workers (they overlap in time)
         self.phase = {"host_proposals": 0.0, "propose_with_dats": 0.0, "select_accept": 0.0}
 
@@ -705,6 +706,7 @@ class HostRound:
 
     def _work(self, w):
         import torch
+        from coulomb_kmc_gb300.workloads import uniform_displacements
         torch.cuda.set_device(self.device)
         pc = time.perf_counter
         rng = self.rngs[w]
@@ -715,7 +717,9 @@ class HostRound:
                 (k, E), (smc, sites, masks, diffs, prop) = self.kmcs[j], self.buf[j]
                 t0 = pc()
                 pos = k.positions if isinstance(k.positions, np.ndarray) else np.asarray(k._positions_host())
-                offlattice_proposals(np.asarray(pos, dtype=np.float64).reshape(-1, 3), E, rng, out=prop)
+                # native generator (the GIL released): the workers draw their systems' proposals at once
+                uniform_displacements(np.asarray(pos, dtype=np.float64).reshape(-1, 3), E, C4_STEP, seed=1000 + j,
+                                      round_=self.round_no, out=prop, threads=1)
                 t1 = pc()
                 k.propose_with_dats(smc, sites, prop, masks, diffs)
                 t2 = pc()
@@ -733,6 +737,7 @@ class HostRound:
         return ph, nprop, h2d, d2h
 
     def run(self):
+        self.round_no += 1
         for ph, nprop, h2d, d2h in self.pool.map(self._work, range(self.workers)):
             for key in ph:
                 self.phase[key] += ph[key]
@@ -1055,6 +1060,8 @@ def cpu_config4(reqs, rounds, warmup, sample=None):
     from oracle import kmc_oracle as ko
     from coulomb_kmc_gb300.lattice import lattice_operator
     from coulomb_kmc_gb300.serving import default_r, system_inputs
+    from coulomb_kmc_gb300.workloads import uniform_displacements
+    cores = os.cpu_count() or 1
     if sample is None:
         # the systems at the 30th and 70th percentile of N of each boundary condition
         sample = []
@@ -1072,11 +1079,14 @@ def cpu_config4(reqs, rounds, warmup, sample=None):
         systems.append((o, E))
     rng = np.random.default_rng(5)
 
+    rnd = [0]
+
     def one_round():
         n_tot = 0
-        for o, E in systems:
+        rnd[0] += 1
+        for si, (o, E) in enumerate(systems):
             n = o.N
-            prop = offlattice_proposals(o.positions, E, rng)
+            prop = uniform_displacements(o.positions, E, C4_STEP, seed=1000 + si, round_=rnd[0], threads=cores)
             d = np.zeros((n, 1))
             o.propose_with_dats(np.array([1], np.int64), np.zeros((n, 1), np.int64), prop,
                                 np.ones((n, 1), np.int64), d)

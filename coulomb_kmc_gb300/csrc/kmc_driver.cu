@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstdint>
 #include <new>
+#include <thread>
 #include <vector>
 
 // a failed CUDA call: its name and error string for kmc_last_error, then KMC_ECUDA
@@ -854,6 +855,50 @@ int kmc_driver_free(kmc_driver *d)
     if (!d) return KMC_EINVAL;
     cudaStreamSynchronize(kmc_int_stream(d->sys));
     release(d);
+    return KMC_OK;
+}
+
+int kmc_host_displacements(int64_t n, const double *pos, double extent, double step, uint64_t seed, int64_t round,
+                           double *out, int32_t nthreads)
+{
+    if (n < 0 || n >= ((int64_t)1 << 32) || (n > 0 && (!pos || !out)) || !(extent > 0.0) || !(step >= 0.0))
+        return KMC_EINVAL;
+    if (n > 0 && out < pos + 3 * n && pos < out + 3 * n) return KMC_EINVAL;
+    const Key key{(uint32_t)seed, (uint32_t)(seed >> 32)};
+    const double half_e = 0.5 * extent;
+    auto work = [&](int64_t a, int64_t b) {
+        for (int64_t i = a; i < b; ++i) {
+            const double x0 = pos[3 * i], y0 = pos[3 * i + 1], z0 = pos[3 * i + 2];
+            double nx = x0, ny = y0, nz = z0;
+            for (int at = 0; at < kMaxAttempts; ++at) {
+                const P4 A = philox((uint32_t)round, (uint32_t)((uint64_t)round >> 32), (uint32_t)i,
+                                    ((uint32_t)at << 4) | TAG_DISP_XY, key.k0, key.k1);
+                const P4 B = philox((uint32_t)round, (uint32_t)((uint64_t)round >> 32), (uint32_t)i,
+                                    ((uint32_t)at << 4) | TAG_DISP_Z, key.k0, key.k1);
+                const double tx = x0 + (2.0 * u53(A.v[0], A.v[1]) - 1.0) * step;
+                const double ty = y0 + (2.0 * u53(A.v[2], A.v[3]) - 1.0) * step;
+                const double tz = z0 + (2.0 * u53(B.v[0], B.v[1]) - 1.0) * step;
+                if (std::fabs(tx) <= half_e && std::fabs(ty) <= half_e && std::fabs(tz) <= half_e) {
+                    nx = tx;
+                    ny = ty;
+                    nz = tz;
+                    break;
+                }
+            }
+            out[3 * i] = nx;
+            out[3 * i + 1] = ny;
+            out[3 * i + 2] = nz;
+        }
+    };
+    const int nt = (int)std::max<int64_t>(1, std::min<int64_t>(std::min(nthreads, 256), (n + 4095) / 4096));
+    if (nt <= 1) {
+        work(0, n);
+        return KMC_OK;
+    }
+    std::vector<std::thread> th;
+    th.reserve(nt);
+    for (int t = 0; t < nt; ++t) th.emplace_back(work, n * t / nt, n * (t + 1) / nt);
+    for (auto &t : th) t.join();
     return KMC_OK;
 }
 

@@ -163,3 +163,22 @@ class OffLatticeSystem:
             self.pos[pid] = prop[pid]
             return pid, True
         return pid, False
+
+
+def uniform_displacements(pos, extent, step, seed, round_, out=None, threads=1):
+    """One proposal per charge for the host path: pos + a uniform displacement in
+    [-step, step]^3, drawn again while it leaves the box (kmc_host_displacements: the
+    device driver's draws for (seed, round, index), native threads, the GIL released).
+    pos: (N, 3) float64; out: an (N, 3) float64 array to write into (for instance the
+    pinned array of KMCFMM.host_buffers)."""
+    import ctypes
+    from . import _native
+    pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+    if out is None:
+        out = np.empty_like(pos)
+    if out.shape != pos.shape or out.dtype != np.float64 or not out.flags.c_contiguous:
+        raise ValueError("out must be a C-contiguous float64 array shaped like pos")
+    _native.check(_native.lib().kmc_host_displacements(pos.shape[0], pos.ctypes.data, float(extent), float(step),
+                                                       ctypes.c_uint64(int(seed)), int(round_), out.ctypes.data,
+                                                       int(threads)), "kmc_host_displacements")
+    return out

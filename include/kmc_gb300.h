@@ -342,6 +342,18 @@ int kmc_bucket_free(kmc_bucket *b);
 int kmc_stream_create(void **stream_out);
 int kmc_stream_destroy(void *stream);
 
+/* Host-side proposal generation for the host path (no reference counterpart; the
+ * reference's example driver draws these in numpy): out[i] = pos[i] + a uniform
+ * displacement in [-step, step]^3, drawn again (up to 32 times, then the old
+ * position) while it leaves the box [-extent/2, extent/2]^3 -- the device driver's
+ * off-lattice draws (Philox4x32-10 keyed by `seed`, counter (round, index,
+ * attempt)), computed on the host with the host's rounding.  n charges, positions
+ * [n][3] in and out (host memory, out may not alias pos), `nthreads` host threads
+ * (<= 0: one).  A pure function of (seed, round, index): the thread count changes
+ * nothing.  Does not touch the GPU. */
+int kmc_host_displacements(int64_t n, const double *pos, double extent, double step, uint64_t seed, int64_t round,
+                           double *out, int32_t nthreads);
+
 /* Diagnostic (no reference counterpart): measured FMA throughput of the
  * current device's FP64 (fp64 != 0) or FP32 pipe in TFLOP/s (FMA = 2 flops),
  * the denominator of the roofline fraction of the FMA-bound kernels. */
