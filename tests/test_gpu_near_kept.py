@@ -122,3 +122,31 @@ def test_kept_potentials_after_extract_and_inject():
     d, _ = _propose(k, 5)
     assert np.max(rel_err(d[1], d[0])) < 1e-11
     k.free()
+
+
+@pytest.mark.parametrize("bc", ["pbc", "27"])
+def test_kept_potentials_two_cells_per_side(bc):
+    """R = 2: every neighbour cell appears twice among a periodic cell's 27 (one image
+    on each side), so the update must take each of them once per image."""
+    n, Rr = 120, 2
+    rng = np.random.default_rng(9)
+    P = rng.uniform(-0.5 * E, 0.5 * E, (n, 3))
+    Q = neutral_charges(n)
+    st = make_state(P, Q, E)
+    k = KMCFMM(st.P, st.Q, st.domain, r=Rr, l=L, boundary_condition=bc)
+    k.initialise()
+    o = ko.OracleKMC(P.copy(), Q, E, Rr, L, bc, lr_operator=lattice_operator(L, E) if bc == "pbc" else None)
+    o.initialise()
+    for i, (pid, new) in enumerate(_moves(rng, P.copy())[:12]):
+        if i % 2:
+            _device_accept(k, pid, new)
+        else:
+            k.accept((pid, new.copy()))
+        o.accept((pid, new.copy()))
+    d, args = _propose(k, 6)
+    assert np.max(rel_err(d[1], d[0])) < 1e-11
+    do = np.zeros_like(d[0])
+    o.propose_with_dats(*args, do)
+    assert np.max(rel_err(d[0], do)) < TOL
+    k.free()
+
