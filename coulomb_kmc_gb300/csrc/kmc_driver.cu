@@ -896,8 +896,18 @@ int kmc_host_displacements(int64_t n, const double *pos, double extent, double s
         return KMC_OK;
     }
     std::vector<std::thread> th;
-    th.reserve(nt);
-    for (int t = 0; t < nt; ++t) th.emplace_back(work, n * t / nt, n * (t + 1) / nt);
+    try {
+        th.reserve(nt);
+        for (int t = 1; t < nt; ++t) th.emplace_back(work, n * t / nt, n * (t + 1) / nt);
+    } catch (...) {
+        // fewer threads than asked (the system refused one): the rest on this thread
+        const int started = (int)th.size() + 1;
+        work(0, n / nt);
+        for (int t = started; t < nt; ++t) work(n * t / nt, n * (t + 1) / nt);
+        for (auto &t : th) t.join();
+        return KMC_OK;
+    }
+    work(0, n / nt);
     for (auto &t : th) t.join();
     return KMC_OK;
 }
