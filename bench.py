@@ -688,9 +688,8 @@ class HostRound:
         self.phase = {"host_proposals": 0.0, "propose_with_dats": 0.0, "select_accept": 0.0}
 
     def close(self):
-        """Free the staging arrays while the workers' streams exist (a pinned array records
-        the streams it was copied on when it is freed), bind every system back to the
-        caller's stream, then end the workers' streams."""
+        """Free the page-locked arrays, bind every system back to the caller's stream, then
+        end the workers' streams."""
         import gc
         import torch
         self.pool.shutdown()

@@ -142,6 +142,8 @@ SIGNATURES = {
     "kmc_drivers_launch": ([c_void_p, c_int64, c_int64, c_void_p, c_void_p, c_int64], c_int),
     "kmc_stream_create": ([POINTER(c_void_p)], c_int),
     "kmc_stream_destroy": ([c_void_p], c_int),
+    "kmc_propose_with_dats_host": ([c_void_p, c_int64, c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
+                                    c_void_p, c_void_p, POINTER(c_int64)], c_int),
     "kmc_host_displacements": ([c_int64, c_void_p, c_double, c_double, ctypes.c_uint64, c_int64, c_void_p, c_int32],
                                c_int),
     "kmc_diag_fma_rate": ([c_int32, c_int32, POINTER(c_double)], c_int),

@@ -30,6 +30,10 @@ struct kmc_system {
     double *d_pos = nullptr, *d_q = nullptr;
     int *d_pcell = nullptr, *d_pslot = nullptr, *d_cnt = nullptr, *d_store_pid = nullptr;
     double *d_phin = nullptr;  // Sys::phin
+    // device copies of the host arrays of kmc_propose_with_dats_host, grown as needed
+    int64_t *hp_smc = nullptr, *hp_sites = nullptr, *hp_mask = nullptr;
+    double *hp_ppos = nullptr, *hp_pq = nullptr, *hp_pde = nullptr;
+    int64_t hp_nsite = 0, hp_n = 0, hp_nm = 0, hp_nq = 0;
     double4_32a *d_store = nullptr;
     double2 *d_lexp = nullptr, *d_mpole = nullptr;
     int *d_ar_ptr = nullptr, *d_ar_col = nullptr, *d_ai_ptr = nullptr, *d_ai_col = nullptr;

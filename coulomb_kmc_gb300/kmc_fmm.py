@@ -214,25 +214,14 @@ class KMCFMM:
         return tuple(out)
 
     # ------------------------------------------------------------------
-    def _staging_pair(self, name, n, torch_dtype):
+    def _pinned(self, name, n, torch_dtype):
+        """A persistent page-locked host array of at least n elements."""
         torch = _torch()
         buf = self._staging.get(name)
-        if buf is None or buf[0].numel() < n:
-            h = torch.empty(max(n, 1), dtype=torch_dtype, pin_memory=True)
-            d = torch.empty(max(n, 1), dtype=torch_dtype, device="cuda")
-            buf = (h, d)
+        if buf is None or buf.numel() < n:
+            buf = torch.empty(max(n, 1), dtype=torch_dtype, pin_memory=True)
             self._staging[name] = buf
         return buf
-
-    def _stage(self, name, arr_np, torch_dtype):
-        """Copy a host array into a persistent pinned -> device staging pair; an array that
-        is the pinned buffer itself (host_buffers) goes to the device without a host copy."""
-        n = arr_np.size
-        h, d = self._staging_pair(name, n, torch_dtype)
-        if arr_np.ctypes.data != h.data_ptr():
-            h[:n].numpy()[:] = arr_np.reshape(-1)
-        d[:n].copy_(h[:n], non_blocking=True)
-        return d
 
     def host_buffers(self, max_prop):
         """Pinned host arrays for the host path of propose_with_dats: prop_positions
@@ -248,15 +237,13 @@ class KMCFMM:
                                      ("prop_masks", "mask", (n, M), torch.int64),
                                      ("current_sites", "sites", (n, 1), torch.int64),
                                      ("prop_energy_diffs", "pde", (n, M), torch.float64)):
-            h, _ = self._staging_pair(name, n * shape[1], dt)
+            h = self._pinned(name, n * shape[1], dt)
             out[key] = h[:n * shape[1]].numpy().reshape(shape)
         return out
 
     def release_host_buffers(self):
-        """Drop the pinned staging arrays (those host_buffers returns) and their device
-        twins; the next host-path call allocates them again.  A caller that ran the host
-        path on CUDA streams it is about to destroy calls this first: a pinned array
-        records, when freed, the streams its copies ran on."""
+        """Drop the page-locked arrays host_buffers returned (the next call to it
+        allocates them again)."""
         self._staging = {}
 
     def propose_with_dats(self, site_max_counts, current_sites, prop_positions, prop_masks, prop_energy_diffs,
@@ -292,26 +279,30 @@ class KMCFMM:
             if sync:
                 self.check_errors()
             return
-        torch = _torch()
-        d_smc = self._stage("smc", _host(smc, np.int64), torch.int64)
-        d_sites = self._stage("sites", _host(sites, np.int64), torch.int64)
-        d_ppos = self._stage("ppos", _host(ppos, np.float64), torch.float64)
-        d_mask = self._stage("mask", _host(pmask, np.int64), torch.int64)
-        d_pde = self._stage("pde", _host(pde, np.float64), torch.float64)
-        d_pq = self._stage("pq", _host(pq, np.float64), torch.float64) if pq is not None else None
-        _native.check(L.kmc_propose_with_dats(self._handle, self.N, M, nsite, d_smc.data_ptr(), d_sites.data_ptr(),
-                                              d_ppos.data_ptr(), d_mask.data_ptr(),
-                                              d_pq.data_ptr() if d_pq is not None else None, d_pde.data_ptr()),
-                      "kmc_propose_with_dats")
-        h_pde = self._staging["pde"][0]
-        n = self.N * M
-        h_pde[:n].copy_(d_pde[:n], non_blocking=True)
-        self.check_errors()  # synchronises the stream
-        out = h_pde[:n].numpy().reshape(pde.shape)
-        if _is_torch(pde):
-            pde.copy_(torch.from_numpy(out))
-        elif pde.ctypes.data != h_pde.data_ptr():  # else the differences already sit in the caller's array
-            pde[...] = out
+        # host arrays: one library call copies them to the device (page-locked ones, as
+        # host_buffers gives, by DMA), evaluates and copies the differences back
+        a_smc = _host(smc, np.int64)
+        a_sites = _host(sites, np.int64)
+        a_ppos = _host(ppos, np.float64)
+        a_mask = _host(pmask, np.int64)
+        a_pq = _host(pq, np.float64) if pq is not None else None
+        direct = (isinstance(pde, np.ndarray) and pde.dtype == np.float64 and pde.flags.c_contiguous
+                  and pde.flags.writeable)
+        a_pde = pde if direct else _host(pde, np.float64).copy()
+        errs = (c_int64 * 2)()
+        _native.check(L.kmc_propose_with_dats_host(self._handle, self.N, M, nsite, a_smc.ctypes.data,
+                                                   a_sites.ctypes.data, a_ppos.ctypes.data, a_mask.ctypes.data,
+                                                   a_pq.ctypes.data if a_pq is not None else None,
+                                                   a_pde.ctypes.data, errs), "kmc_propose_with_dats_host")
+        if errs[1] > 0:
+            raise RuntimeError("A cell store overflowed during a device-selected accept.")
+        if errs[0] > 0:
+            raise RuntimeError("Bad proposed move was detected.")
+        if not direct:
+            if _is_torch(pde):
+                pde.copy_(_torch().from_numpy(a_pde.reshape(tuple(pde.shape))))
+            else:
+                pde[...] = a_pde.reshape(pde.shape)
 
     def error_counts(self):
         """(invalid proposed moves, store overflows) counted on the device since the last

@@ -100,6 +100,20 @@ int kmc_propose_with_dats(kmc_system *s, int64_t n, int64_t max_prop, int64_t n_
                           const double *prop_positions, const int64_t *prop_masks, const double *prop_charges,
                           double *prop_energy_diffs);
 
+/* The same call with every array in host memory, as the reference's
+ * propose_with_dats takes its dats: the arrays (prop_energy_diffs too, whose
+ * inactive slots keep their values) go to device buffers the handle keeps, the
+ * differences come back into prop_energy_diffs, and the call returns when they
+ * are there.  errors_out[0] receives the number of invalid moves and errors_out[1]
+ * the store overflows counted since the last read (both read and cleared, as
+ * kmc_get_error does).  Page-locked host arrays make the copies asynchronous DMA.
+ * One library call per propose, so a caller's language runtime takes no part in
+ * the copies. */
+int kmc_propose_with_dats_host(kmc_system *s, int64_t n, int64_t max_prop, int64_t n_site_types,
+                               const int64_t *site_max_counts, const int64_t *current_sites,
+                               const double *prop_positions, const int64_t *prop_masks, const double *prop_charges,
+                               double *prop_energy_diffs, int64_t *errors_out);
+
 /* Energy differences for explicit moves in CSR form (host memory):
  * particle ids pids[nump], exclusive_sum[nump+1], new_positions[total][3];
  * diffs_out[total] receives dE * energy_unit (host).  Synchronises.

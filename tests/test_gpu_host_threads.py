@@ -6,9 +6,8 @@ so one system's host work overlaps another's device work).  The same calls made
 from four threads on four dedicated streams must give, bit for bit, what they
 give one after another on the caller's stream: propose_with_dats through the
 pinned host arrays, a Metropolis accept, three rounds.  Afterwards the systems'
-staging arrays are released, the streams destroyed and the systems freed, and
-the process carries on (a pinned array records the streams it was copied on when
-it is freed, so it must go before they do).
+page-locked arrays are released, the streams destroyed and the systems freed,
+and the process carries on.
 """
 import threading
 
