@@ -46,3 +46,9 @@ def test_python_api_surface():
     with pytest.raises(NotImplementedError):
         ck.KMCFMM(ck.dats.PositionDat(4), ck.dats.ParticleDat(4), ck.dats.Domain(4.0),
                   boundary_condition="ff-only")
+
+
+def test_host_propose_rejects_a_null_handle_without_gpu_work():
+    lib = _native.lib()
+    errs = (ctypes.c_int64 * 2)()
+    assert lib.kmc_propose_with_dats_host(None, 1, 1, 1, None, None, None, None, None, None, errs) == -1
